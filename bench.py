@@ -1,0 +1,393 @@
+"""Benchmark of the butterfly Helmholtz apply on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl bfg|reference]
+                    [--config c4|c2|c1] [--rhs R]
+
+One step = one apply of the factorization to R right-hand sides (the
+workload's synthetic, seeded inputs).  The metric is right-hand sides per
+second at <= 1e-6 relative error against a dense FP64 product on sampled
+rows: the fastest precision whose error meets that bound is the headline.
+The factorization itself runs once before timing (its time is reported).
+
+--impl reference times the reference's own apply algorithm on the host cores
+(the C port of the oracle, fed the same block structure) -- the reference
+library compiled from source cannot be present on this machine.
+
+Multi-GPU runs are independent replicas (the path needs no exchange): each
+rank runs the same workload, value = total RHS / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# workloads (sizes, geometry, wavenumber, tolerance) and the error bound
+CONFIGS = {
+    # 4,096 uniform sources / circle r=3 targets, k=64, leaf 64, tol 1e-8, 1 RHS
+    "c1": dict(n=4096, k=64.0, curve="circle", a=3.0, b=3.0, leaf=64, tol=1e-8, R=1),
+    # 65,536 / ellipse (3,2), k=512, tol 1e-10, 16 RHS
+    "c2": dict(n=65536, k=512.0, curve="ellipse", a=3.0, b=2.0, leaf=64, tol=1e-10, R=16),
+    # 262,144 / star r = 3 + 0.5 cos 5 theta, k=2048, tol 1e-7, 256 RHS
+    "c4": dict(n=262144, k=2048.0, curve="star", a=3.0, b=3.0, leaf=64, tol=1e-7, R=256),
+}
+METRIC = "Butterfly apply RHS/s at 1e-6 rel err vs plain FP64 GPU; GMRES time-to-1e-8"
+ERR_BOUND = 1e-6
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="bfg", choices=["bfg", "reference"])
+    ap.add_argument("--config", default=os.environ.get("BFG_BENCH_CONFIG", "c2"),
+                    choices=sorted(CONFIGS))
+    ap.add_argument("--rhs", type=int, default=0)
+    ap.add_argument("--dense-rows", type=int, default=512)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload_inputs(cfg, impl):
+    """Sources iid uniform in [-1,1]^2 (seed 0), targets equispaced in the
+    curve parameter."""
+    if impl == "bfg":
+        import butterfly_gb300 as B
+        src = B.uniform_square_points(cfg["n"], 0)
+        tgt = B.curve_points(cfg["curve"], cfg["n"], cfg["a"], cfg["b"])
+    else:
+        from oracle import bf_oracle as O
+        src = O.uniform_square_points(cfg["n"], 0)
+        tgt = O.curve_points(cfg["curve"], cfg["n"], cfg["a"], cfg["b"])
+    return src, tgt
+
+
+def config_json(name, cfg, R):
+    return {"workload": "helmholtz2d_butterfly_apply_%s" % name, "n_src": cfg["n"],
+            "n_tgt": cfg["n"], "k": cfg["k"], "targets": cfg["curve"], "leaf_size": cfg["leaf"],
+            "tolerance": cfg["tol"], "rhs": R,
+            "l2": "factor arena and vectors larger than L2 (129 MB); no flush needed"}
+
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.proc = None
+        self.lines = []
+        self.device = device
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("BFG_BENCH_GLOO") is None else "gloo")
+        return world, rank, local, dist
+    return 1, 0, 0, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(v, dist):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# CPU legs (the only place bench.py runs the oracle)
+# ---------------------------------------------------------------------------
+def cpu_port_time(plan_text, data, col_major, X, nthreads, budget_s=20.0):
+    """RHS/s of the reference's apply algorithm (oracle port) on host cores,
+    on a bounded number of RHS."""
+    from oracle import bf_oracle as O
+    port = O.ApplyPort.from_plan(plan_text, data, col_major)
+    t0 = time.perf_counter()
+    port(X[:, :1], nthreads)
+    t1 = time.perf_counter() - t0
+    # grow the sample while it stays within the budget
+    Rs = int(max(1, min(X.shape[1], budget_s / 3 / max(t1, 1e-6))))
+    Xs = np.ascontiguousarray(X[:, :Rs])
+    times = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        port(Xs, nthreads)
+        times.append(time.perf_counter() - t0)
+    t = float(np.median(times))
+    return Rs / t, Rs, t
+
+
+def run_reference(args):
+    """--impl reference: the reference's apply (oracle C port of
+    mat_block_dense/mat_product/mat_block_diag/mat_block_coo Mul) on host
+    cores over the same block structure, built by the oracle planner."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import bf_oracle as O
+    cfg = CONFIGS[args.config]
+    R = args.rhs or cfg["R"]
+    src, tgt = workload_inputs(cfg, "reference")
+    t0 = time.perf_counter()
+    fac = O.Factorization(O.Helm2(cfg["k"]), src, tgt, leaf_size=cfg["leaf"], eps=cfg["tol"],
+                          fill=False)
+    plan_s = time.perf_counter() - t0
+    text = fac.plan_text()
+    entries = fac.num_entries()
+    # block values do not change the apply's cost; a constant fill stands in
+    # for the factorization (seconds to hours on the CPU)
+    data = np.full(entries, 1e-3 + 1e-3j, dtype=np.complex128)
+    rng = O.RefRng(1)
+    Xs = rng.complex_randn(cfg["n"] * 1).reshape(cfg["n"], 1)
+    Xs = np.ascontiguousarray(np.repeat(Xs, R, axis=1))
+    nthreads = os.cpu_count() or 1
+    port = O.ApplyPort.from_plan(text, data, False)
+    port(Xs[:, :1], nthreads)
+    t0 = time.perf_counter()
+    port(Xs[:, :1], nthreads)
+    t1 = time.perf_counter() - t0
+    Rs = int(max(1, min(R, 8.0 / max(t1, 1e-6))))
+    times = []
+    for _ in range(max(1, args.warmup)):
+        port(Xs[:, :Rs], nthreads)
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        port(Xs[:, :Rs], nthreads)
+        times.append(time.perf_counter() - t0)
+    ms = float(np.mean(times)) * 1e3
+    value = Rs / (ms / 1e3)
+    sample = ("all %d blocks of the factorization's structure (oracle planner, constant "
+              "block values), %d of %d RHS per step" % (len(fac.blocks()), Rs, R))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "RHS/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "complex128", "data": "synthetic",
+            "config": config_json(args.config, cfg, R),
+            "cpu_baseline": {"value": value, "unit": "RHS/s", "cores": nthreads,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "RHS/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "plan_s": plan_s, "world_size": world}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+
+    import butterfly_gb300 as B
+
+    world, rank, local, dist = dist_setup()
+    torch.cuda.set_device(local)
+    cfg = CONFIGS[args.config]
+    R = args.rhs or cfg["R"]
+    n = cfg["n"]
+    ctx = B.Context(local)
+    src, tgt = workload_inputs(cfg, "bfg")
+
+    t0 = time.perf_counter()
+    fac = B.FacHelm2.make_multilevel(
+        B.Helm2(cfg["k"]), B.Quadtree(src, leaf_size=cfg["leaf"]),
+        B.Quadtree(tgt, leaf_size=cfg["leaf"]), rank_eps=cfg["tol"], pinv_tol=cfg["tol"],
+        context=ctx)
+    fac_wall_s = time.perf_counter() - t0
+    st = fac.stats()
+
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    rng = B.Rng(1234 + rank)
+    Xh = rng.complex_randn(n * R).reshape(n, R)
+    with torch.cuda.stream(stream):
+        X64 = torch.from_numpy(Xh).to("cuda")
+        X32 = X64.to(torch.complex64)
+        Y64 = torch.empty((n, R), dtype=torch.complex128, device="cuda")
+        Y32 = torch.empty((n, R), dtype=torch.complex64, device="cuda")
+    stream.synchronize()
+
+    # accuracy: dense FP64 rows on the GPU (the product's FP64 kernel
+    # evaluator; validated against the CPU oracle in the tests)
+    Re = min(R, 16)
+    rows = np.unique(np.linspace(0, n - 1, min(args.dense_rows, n)).astype(np.int64))
+    with torch.cuda.stream(stream):
+        Xe = X64[:, :Re].contiguous()
+        yd = fac.dense_rows(rows, Xe, Re)
+    stream.synchronize()
+    yd = yd.cpu().numpy()
+
+    precs = {"fp64": (X64, Y64), "fp32": (X32, Y32)}
+    errs = {}
+    for p, (X, Y) in precs.items():
+        fac.apply_device(X.data_ptr(), R, R, Y.data_ptr(), R, p)
+        stream.synchronize()
+        ye = Y[rows][:, :Re].cpu().numpy().astype(np.complex128)
+        errs[p] = float(np.linalg.norm(ye - yd) / np.linalg.norm(yd))
+
+    def timed(p):
+        X, Y = precs[p]
+        for _ in range(max(3, args.warmup)):
+            fac.apply_device(X.data_ptr(), R, R, Y.data_ptr(), R, p)
+        stream.synchronize()
+        barrier(dist)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fac.apply_device(X.data_ptr(), R, R, Y.data_ptr(), R, p)
+        e1.record(stream)
+        e1.synchronize()
+        torch.cuda.synchronize()
+        barrier(dist)
+        return e0.elapsed_time(e1)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    total_ms = {p: timed(p) for p in precs}
+    clk = clocks.stop()
+    total_ms = {p: max_over_ranks(v, dist) for p, v in total_ms.items()}
+    rhs_s = {p: world * R * args.steps / (total_ms[p] / 1e3) for p in precs}
+    ok = [p for p in precs if errs[p] <= ERR_BOUND]
+    head = max(ok, key=lambda p: rhs_s[p]) if ok else "fp64"
+
+    # roofline of the dominant launch of the headline precision
+    X, Y = precs[head]
+    per = []
+    for _ in range(3):
+        per.append(fac.apply_timed(X.data_ptr(), R, R, Y.data_ptr(), R, head))
+    per = np.mean(np.array(per), axis=0)
+    info = fac.launch_info()
+    dom = int(np.argmax(per))
+    sA = 16 if head == "fp64" else 8
+    sv = 16 if head == "fp64" else 8
+    alg_bytes = float(info[dom, 0] * sA + R * sv * (info[dom, 1] + info[dom, 2]))
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        peak, peak_src = 6800.0, "fallback"
+    achieved = alg_bytes / (per[dom] / 1e3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
+            "kernel": "apply launch %d of %d" % (dom, len(per)),
+            "launch_ms": float(per[dom]),
+            "fp64_flops_per_s": float(8.0 * info[dom, 0] * R / (per[dom] / 1e3))}
+
+    # end to end through the C ABI with pinned host complex128 operands
+    Xp = torch.from_numpy(Xh).pin_memory()
+    Yp = torch.empty((n, R), dtype=torch.complex128).pin_memory()
+    xp, yp = Xp.data_ptr(), Yp.data_ptr()
+    lib = B.lib()
+    for _ in range(2):
+        ctx.check(lib.bfgFacApplyHost(fac.handle, B.PRECISIONS[head], B._VP(xp), R, R,
+                                      B._VP(yp), R, 0))
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.check(lib.bfgFacApplyHost(fac.handle, B.PRECISIONS[head], B._VP(xp), R, R,
+                                      B._VP(yp), R, 0))
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
+    e2e = {"value": world * R * args.steps / e2e_s, "unit": "RHS/s",
+           "h2d_bytes_per_step": n * R * 16, "d2h_bytes_per_step": n * R * 16,
+           "precision": head}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        tab, ent = fac.blocks()
+        nthreads = os.cpu_count() or 1
+        v, Rs, t = cpu_port_time(fac.describe(), ent, True, Xh, nthreads)
+        cpu = {"value": v, "unit": "RHS/s", "cores": nthreads, "kind": "port",
+               "sample": "full operator (%d blocks, this factorization), %d RHS, median of 3"
+                         % (len(tab), Rs)}
+
+    if rank != 0:
+        return
+    launches = len(fac.launch_info()) * args.steps
+    line = {"metric": METRIC, "value": rhs_s[head], "unit": "RHS/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms[head] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "complex64" if head == "fp32" else "complex128",
+            "data": "synthetic", "config": config_json(args.config, cfg, R),
+            "precision": head, "rel_err": errs[head], "rel_err_all": errs,
+            "rhs_per_s_all": rhs_s, "err_bound": ERR_BOUND,
+            "err_rows": int(len(rows)), "err_rhs": Re,
+            "fp64_speedup": rhs_s[head] / rhs_s["fp64"],
+            "factorization": {"wall_s": fac_wall_s, "device_ms": st["factorMs"],
+                              "blocks": st["numBlocks"], "bytes_fp64": fac.num_bytes(),
+                              "max_rank": st["maxRank"],
+                              "jacobi_not_converged": st["jacobiNotConverged"]},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "gpu_launches": launches}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

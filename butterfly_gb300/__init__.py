@@ -1,0 +1,511 @@
+"""butterfly_gb300 -- GB300-native multilevel butterfly factorization of the
+2-D Helmholtz kernel G(x, y) = (i/4) H0(k |x - y|), and its application to
+vectors, on one GPU.
+
+The Python surface mirrors the reference's Cython wrapper
+(wrappers/python/butterfly.pyx): ``Helm2`` (273-305), ``LayerPot`` (330-354),
+``FacHelm2.make_multilevel`` (211-220) and ``Mat.__matmul__`` (384-396).
+Everything runs through the C ABI of ``libbfg.so`` (include/bfg.h); there is
+no CPU fallback -- without the compiled library every call raises.
+"""
+from __future__ import annotations
+
+import atexit
+import ctypes
+import enum
+import os
+import weakref
+from dataclasses import dataclass
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libbfg.so")
+
+BFG_OK = 0
+APPLY_ORIGINAL_ORDER = 1
+PRECISIONS = {"fp64": 0, "fp32": 1}
+STATUS_NAMES = {0: "OK", 1: "INVALID_ARGUMENTS", 2: "RUNTIME", 3: "NOT_IMPLEMENTED",
+                4: "MEMORY", 5: "OUT_OF_RANGE", 8: "INCOMPATIBLE_SHAPES", 32: "CUDA",
+                33: "TIMEOUT", 34: "NUMERICAL"}
+
+
+class BfgError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__("%s (%d): %s" % (STATUS_NAMES.get(status, "?"), status, message))
+        self.status = status
+
+
+class _Helm2C(ctypes.Structure):
+    _fields_ = [("k", ctypes.c_double), ("layerPot", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("alphaRe", ctypes.c_double),
+                ("alphaIm", ctypes.c_double), ("betaRe", ctypes.c_double),
+                ("betaIm", ctypes.c_double)]
+
+
+class _FacOptionsC(ctypes.Structure):
+    _fields_ = [("leafSize", ctypes.c_int64), ("rankEps", ctypes.c_double),
+                ("pinvCut", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("pinvTol", ctypes.c_double)]
+
+
+class _FacStatsC(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int64) for n in (
+        "numRows", "numCols", "numBlocks", "numFirst", "numMiddle", "numLast",
+        "numDense", "numProducts", "arenaEntries", "numStages", "numItems",
+        "maxRank", "jacobiNotConverged")] + [("factorMs", ctypes.c_double),
+                                             ("flopsPerRhs", ctypes.c_double)]
+
+
+class _RngC(ctypes.Structure):
+    _fields_ = [("s", ctypes.c_uint64 * 4)]
+
+
+_lib = None
+_VP = ctypes.c_void_p
+_I64 = ctypes.c_int64
+
+
+def lib() -> ctypes.CDLL:
+    """The compiled library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise BfgError(2, "libbfg.so is missing; run __graft_entry__.build() "
+                          "(or python -m butterfly_gb300.build)")
+    L = ctypes.CDLL(LIB_PATH)
+    sig = {
+        "bfgContextCreate": [ctypes.c_int32, ctypes.POINTER(_VP)],
+        "bfgContextDestroy": [_VP],
+        "bfgContextSetStream": [_VP, _VP],
+        "bfgContextGetStream": [_VP, ctypes.POINTER(_VP)],
+        "bfgContextSynchronize": [_VP],
+        "bfgFacOptionsDefault": [ctypes.POINTER(_FacOptionsC)],
+        "bfgFacHelm2MakeMultilevel": [_VP, ctypes.POINTER(_Helm2C), _VP, _VP, _I64, _VP, _VP,
+                                      _I64, ctypes.POINTER(_FacOptionsC), ctypes.POINTER(_VP)],
+        "bfgFacDestroy": [_VP],
+        "bfgFacGetShape": [_VP, ctypes.POINTER(_I64), ctypes.POINTER(_I64)],
+        "bfgFacGetPerms": [_VP, _VP, _VP],
+        "bfgFacNumBytes": [_VP, ctypes.POINTER(_I64)],
+        "bfgFacGetStats": [_VP, ctypes.POINTER(_FacStatsC)],
+        "bfgFacDescribe": [_VP, ctypes.c_char_p, _I64, ctypes.POINTER(_I64)],
+        "bfgFacCopyBlocks": [_VP, _VP, _I64, _VP, _I64],
+        "bfgFacApply": [_VP, ctypes.c_int, _VP, _I64, _I64, _VP, _I64, ctypes.c_uint32],
+        "bfgFacApplyHost": [_VP, ctypes.c_int, _VP, _I64, _I64, _VP, _I64, ctypes.c_uint32],
+        "bfgFacApplyTimed": [_VP, ctypes.c_int, _VP, _I64, _I64, _VP, _I64, ctypes.c_uint32,
+                             _VP, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)],
+        "bfgFacDenseRows": [_VP, _VP, _I64, _VP, _I64, _I64, _VP, _I64],
+        "bfgFacGetLaunchInfo": [_VP, ctypes.c_uint32, _VP, ctypes.c_int32,
+                                ctypes.POINTER(ctypes.c_int32)],
+        "bfgHelm2KernelMatrix": [_VP, ctypes.POINTER(_Helm2C), _VP, _VP, _I64, _VP, _VP, _I64,
+                                 _VP],
+        "bfgBessel01": [_VP, _VP, _I64, _VP],
+        "bfgPlanHelm2": [ctypes.c_double, _VP, _I64, _VP, _I64, ctypes.POINTER(_FacOptionsC),
+                         _VP, _VP, ctypes.c_char_p, _I64, ctypes.POINTER(_I64)],
+        "bfgBessel01Host": [_VP, _I64, _VP],
+        "bfgRngSeed": [ctypes.POINTER(_RngC), ctypes.c_uint64],
+        "bfgRngUniform1": [ctypes.POINTER(_RngC)],
+        "bfgRngUniform": [ctypes.POINTER(_RngC), _I64, _VP],
+        "bfgRngComplexRandn": [ctypes.POINTER(_RngC), _I64, _VP],
+    }
+    for name, args in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    L.bfgGetErrorString.argtypes = [_VP]
+    L.bfgGetErrorString.restype = ctypes.c_char_p
+    L.bfgFacOptionsDefault.restype = None
+    L.bfgRngSeed.restype = None
+    L.bfgRngUniform.restype = None
+    L.bfgRngComplexRandn.restype = None
+    L.bfgRngUniform1.restype = ctypes.c_double
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return None if a is None else _VP(a.ctypes.data)
+
+
+# ---------------------------------------------------------------------------
+class Context:
+    """One CUDA device and one stream (bfgContextCreate)."""
+
+    def __init__(self, device: int = 0):
+        h = _VP()
+        st = lib().bfgContextCreate(device, ctypes.byref(h))
+        if st != BFG_OK:
+            raise BfgError(st, "could not create a context on device %d" % device)
+        self.handle = h
+        self.device = device
+        _live_contexts.add(self)
+
+    def check(self, st: int, what: str = ""):
+        if st != BFG_OK:
+            msg = lib().bfgGetErrorString(self.handle).decode()
+            raise BfgError(st, (what + ": " if what else "") + msg)
+
+    def set_stream(self, cuda_stream_ptr: int | None):
+        """Launch on this cudaStream_t (0 = CUDA's legacy default stream)."""
+        self.check(lib().bfgContextSetStream(self.handle, _VP(cuda_stream_ptr or 0)))
+
+    def get_stream(self) -> int:
+        v = _VP()
+        self.check(lib().bfgContextGetStream(self.handle, ctypes.byref(v)))
+        return v.value or 0
+
+    def synchronize(self):
+        self.check(lib().bfgContextSynchronize(self.handle))
+
+    def on_stream(self, cuda_stream_ptr: int):
+        """Context manager: launch on the given stream, then restore."""
+        ctx = self
+
+        class _On:
+            def __enter__(self_):
+                self_.prev = ctx.get_stream()
+                ctx.set_stream(cuda_stream_ptr)
+
+            def __exit__(self_, *exc):
+                ctx.set_stream(self_.prev)
+
+        return _On()
+
+    def close(self):
+        if getattr(self, "handle", None) and _lib is not None:
+            _lib.bfgContextDestroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        self.close()
+
+
+_default_ctx = {}
+_live_contexts = weakref.WeakSet()
+_live_facs = weakref.WeakSet()
+
+
+def _release_all():
+    """Destroy every factorization, then every context, before the CUDA
+    runtime is torn down at interpreter exit."""
+    for f in list(_live_facs):
+        f.close()
+    for c in list(_live_contexts):
+        c.close()
+    _default_ctx.clear()
+
+
+atexit.register(_release_all)
+
+
+def default_context(device: int = 0) -> Context:
+    if device not in _default_ctx:
+        _default_ctx[device] = Context(device)
+    return _default_ctx[device]
+
+
+class LayerPot(enum.IntEnum):
+    """BfLayerPotential (layer_pot.h:52-65)."""
+    Single = 1
+    PvDouble = 2
+    PvNormalDerivSingle = 3
+    CombinedField = 5
+    S = 1
+    D = 2
+    Sp = 3
+
+
+@dataclass
+class Helm2:
+    """BfHelm2 (helm2.h:10-15)."""
+    k: float
+    layer_pot: LayerPot = LayerPot.Single
+    alpha: complex = 0j
+    beta: complex = 0j
+
+    def _c(self) -> _Helm2C:
+        return _Helm2C(float(self.k), int(self.layer_pot), 0, self.alpha.real,
+                       self.alpha.imag, self.beta.real, self.beta.imag)
+
+
+@dataclass
+class Quadtree:
+    """Points (N, 2) with optional unit normals; the library builds the tree
+    with the reference's rule (quadtree.c:80-98) when factorizing."""
+    points: np.ndarray
+    normals: np.ndarray | None = None
+    leaf_size: int = 1
+
+
+def _xy(a):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if a.ndim != 2 or a.shape[1] != 2:
+        raise ValueError("points/normals must have shape (N, 2)")
+    return a
+
+
+class FacHelm2:
+    """bfFacHelm2MakeMultilevel (fac_helm2.c:943-1002) on the GPU."""
+
+    def __init__(self):
+        raise TypeError("FacHelm2 can't be instantiated")
+
+    @staticmethod
+    def make_multilevel(helm: Helm2, src_tree: Quadtree, tgt_tree: Quadtree | None = None,
+                        *, rank_eps: float = 1e-15, pinv_tol: float | None = None,
+                        context: Context | None = None) -> "Fac":
+        tgt_tree = src_tree if tgt_tree is None else tgt_tree
+        if src_tree.leaf_size != tgt_tree.leaf_size:
+            raise ValueError("both trees must use the same leaf size")
+        ctx = context or default_context()
+        src, tgt = _xy(src_tree.points), _xy(tgt_tree.points)
+        sn, tn = _xy(src_tree.normals), _xy(tgt_tree.normals)
+        opts = _FacOptionsC()
+        lib().bfgFacOptionsDefault(ctypes.byref(opts))
+        opts.leafSize = int(src_tree.leaf_size)
+        opts.rankEps = float(rank_eps)
+        if pinv_tol is not None:
+            opts.pinvCut, opts.pinvTol = 1, float(pinv_tol)
+        h = _VP()
+        hc = helm._c()
+        ctx.check(lib().bfgFacHelm2MakeMultilevel(
+            ctx.handle, ctypes.byref(hc), _ptr(src), _ptr(sn), len(src), _ptr(tgt), _ptr(tn),
+            len(tgt), ctypes.byref(opts), ctypes.byref(h)), "make_multilevel")
+        return Fac(ctx, h, helm)
+
+
+class Fac:
+    """A GPU-resident butterfly factorization: the BfMat returned by
+    bfFacHelm2MakeMultilevel, with ``@`` = bfMatMul (mat.c:183-185)."""
+
+    def __init__(self, ctx: Context, handle, helm: Helm2):
+        self.ctx, self.handle, self.helm = ctx, handle, helm
+        _live_facs.add(self)
+        r, c = _I64(), _I64()
+        ctx.check(lib().bfgFacGetShape(handle, ctypes.byref(r), ctypes.byref(c)))
+        self.shape = (r.value, c.value)
+        self._perms = None
+
+    def close(self):
+        if getattr(self, "handle", None) and _lib is not None:
+            _lib.bfgFacDestroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        self.close()
+
+    # -- structure ---------------------------------------------------------
+    def perms(self):
+        if self._perms is None:
+            sp = np.empty(self.shape[1], dtype=np.int64)
+            tp = np.empty(self.shape[0], dtype=np.int64)
+            self.ctx.check(lib().bfgFacGetPerms(self.handle, _ptr(sp), _ptr(tp)))
+            self._perms = (sp, tp)
+        return self._perms
+
+    @property
+    def src_perm(self):
+        return self.perms()[0]
+
+    @property
+    def tgt_perm(self):
+        return self.perms()[1]
+
+    def num_bytes(self) -> int:
+        v = _I64()
+        self.ctx.check(lib().bfgFacNumBytes(self.handle, ctypes.byref(v)))
+        return v.value
+
+    def stats(self) -> dict:
+        s = _FacStatsC()
+        self.ctx.check(lib().bfgFacGetStats(self.handle, ctypes.byref(s)))
+        return {name: getattr(s, name) for name, _ in s._fields_}
+
+    def describe(self) -> str:
+        n = _I64()
+        self.ctx.check(lib().bfgFacDescribe(self.handle, None, 0, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(n.value + 1)
+        self.ctx.check(lib().bfgFacDescribe(self.handle, buf, n.value + 1, ctypes.byref(n)))
+        return buf.value.decode()
+
+    def blocks(self):
+        """(table, entries): table rows (kind, m, n, offset), entries the
+        complex128 arena (each block column-major)."""
+        st = self.stats()
+        ent = np.empty(max(1, st["arenaEntries"]), dtype=np.complex128)
+        tab = np.empty((st["numBlocks"], 4), dtype=np.int64)
+        self.ctx.check(lib().bfgFacCopyBlocks(self.handle, _ptr(ent), st["arenaEntries"],
+                                              _ptr(tab), st["numBlocks"]))
+        return tab, ent
+
+    # -- apply -------------------------------------------------------------
+    def apply(self, X, precision: str = "fp64", original_order: bool = False):
+        """Y = A X.  numpy complex128 X -> host path (copies inside);
+        torch CUDA X -> device path on the context's stream."""
+        prec = PRECISIONS[precision]
+        flags = APPLY_ORIGINAL_ORDER if original_order else 0
+        if isinstance(X, np.ndarray):
+            squeeze = X.ndim == 1
+            Xh = np.ascontiguousarray(X.reshape(X.shape[0], -1), dtype=np.complex128)
+            if Xh.shape[0] != self.shape[1]:
+                raise ValueError("X has %d rows, expected %d" % (Xh.shape[0], self.shape[1]))
+            R = Xh.shape[1]
+            Y = np.empty((self.shape[0], R), dtype=np.complex128)
+            self.ctx.check(lib().bfgFacApplyHost(self.handle, prec, _ptr(Xh), R, R, _ptr(Y), R,
+                                                 flags), "apply")
+            return Y[:, 0] if squeeze else Y
+        import torch
+        squeeze = X.dim() == 1
+        Xd = X.reshape(X.shape[0], -1)
+        want = torch.complex128 if precision == "fp64" else torch.complex64
+        if Xd.dtype != want or not Xd.is_contiguous():
+            Xd = Xd.to(want).contiguous()
+        if Xd.shape[0] != self.shape[1]:
+            raise ValueError("X has %d rows, expected %d" % (Xd.shape[0], self.shape[1]))
+        R = Xd.shape[1]
+        Y = torch.empty((self.shape[0], R), dtype=want, device=Xd.device)
+        # run on torch's current stream so torch work before and after is ordered
+        with self.ctx.on_stream(torch.cuda.current_stream(Xd.device).cuda_stream):
+            self.apply_device(Xd.data_ptr(), R, R, Y.data_ptr(), R, precision, original_order)
+        return Y[:, 0] if squeeze else Y
+
+    def apply_device(self, x_ptr: int, ldx: int, R: int, y_ptr: int, ldy: int,
+                     precision: str = "fp64", original_order: bool = False):
+        flags = APPLY_ORIGINAL_ORDER if original_order else 0
+        self.ctx.check(lib().bfgFacApply(self.handle, PRECISIONS[precision], _VP(x_ptr), ldx, R,
+                                         _VP(y_ptr), ldy, flags), "apply")
+
+    def apply_timed(self, x_ptr: int, ldx: int, R: int, y_ptr: int, ldy: int,
+                    precision: str = "fp64", original_order: bool = False):
+        """Per-launch device milliseconds of one apply."""
+        flags = APPLY_ORIGINAL_ORDER if original_order else 0
+        cap = 256
+        ms = np.zeros(cap, dtype=np.float32)
+        n = ctypes.c_int32()
+        self.ctx.check(lib().bfgFacApplyTimed(self.handle, PRECISIONS[precision], _VP(x_ptr), ldx,
+                                              R, _VP(y_ptr), ldy, flags, _ptr(ms), cap,
+                                              ctypes.byref(n)), "apply_timed")
+        return ms[:n.value].copy()
+
+    def launch_info(self, original_order: bool = False) -> np.ndarray:
+        """(entries, rows_in, rows_out) per launch of one apply."""
+        cap = 256
+        info = np.zeros((cap, 3), dtype=np.int64)
+        n = ctypes.c_int32()
+        self.ctx.check(lib().bfgFacGetLaunchInfo(
+            self.handle, APPLY_ORIGINAL_ORDER if original_order else 0, _ptr(info), cap,
+            ctypes.byref(n)), "launch_info")
+        return info[:n.value].copy()
+
+    def __matmul__(self, X):
+        return self.apply(X)
+
+    def dense_rows(self, rows, X_dev, R: int):
+        """Rows (tree order) of K X in FP64 on the GPU; X_dev a torch
+        complex128 CUDA tensor (tree order)."""
+        import torch
+        rows = np.ascontiguousarray(rows, dtype=np.int64)
+        out = torch.empty((len(rows), R), dtype=torch.complex128, device=X_dev.device)
+        with self.ctx.on_stream(torch.cuda.current_stream(X_dev.device).cuda_stream):
+            self.ctx.check(lib().bfgFacDenseRows(self.handle, _ptr(rows), len(rows),
+                                                 _VP(X_dev.data_ptr()), R, R,
+                                                 _VP(out.data_ptr()), R), "dense_rows")
+        return out
+
+
+def kernel_matrix(helm: Helm2, src, tgt, src_normals=None, tgt_normals=None,
+                  context: Context | None = None) -> np.ndarray:
+    """bfHelm2GetKernelMatrix (helm2.c:282-319) evaluated on the GPU."""
+    ctx = context or default_context()
+    src, tgt = _xy(src), _xy(tgt)
+    sn, tn = _xy(src_normals), _xy(tgt_normals)
+    out = np.empty((len(tgt), len(src)), dtype=np.complex128)
+    hc = helm._c()
+    ctx.check(lib().bfgHelm2KernelMatrix(ctx.handle, ctypes.byref(hc), _ptr(src), _ptr(sn),
+                                         len(src), _ptr(tgt), _ptr(tn), len(tgt), _ptr(out)),
+              "kernel_matrix")
+    return out
+
+
+def bessel01(x, context: Context | None = None) -> np.ndarray:
+    """(J0, Y0, J1, Y1) at x > 0 from the device evaluator."""
+    ctx = context or default_context()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty((len(x), 4))
+    ctx.check(lib().bfgBessel01(ctx.handle, _ptr(x), len(x), _ptr(out)), "bessel01")
+    return out
+
+
+def plan_helm2(k: float, src, tgt, leaf_size: int = 1, rank_eps: float = 1e-15):
+    """Host-only: (src_perm, tgt_perm, plan_text) of the factorization the
+    library would build -- no GPU involved."""
+    src, tgt = _xy(src), _xy(tgt)
+    opts = _FacOptionsC()
+    lib().bfgFacOptionsDefault(ctypes.byref(opts))
+    opts.leafSize, opts.rankEps = int(leaf_size), float(rank_eps)
+    sp = np.empty(len(src), dtype=np.int64)
+    tp = np.empty(len(tgt), dtype=np.int64)
+    n = _I64()
+    st = lib().bfgPlanHelm2(float(k), _ptr(src), len(src), _ptr(tgt), len(tgt),
+                            ctypes.byref(opts), _ptr(sp), _ptr(tp), None, 0, ctypes.byref(n))
+    if st != BFG_OK:
+        raise BfgError(st, "plan_helm2 failed")
+    buf = ctypes.create_string_buffer(n.value + 1)
+    st = lib().bfgPlanHelm2(float(k), _ptr(src), len(src), _ptr(tgt), len(tgt),
+                            ctypes.byref(opts), None, None, buf, n.value + 1, ctypes.byref(n))
+    if st != BFG_OK:
+        raise BfgError(st, "plan_helm2 failed")
+    return sp, tp, buf.value.decode()
+
+
+def bessel01_host(x) -> np.ndarray:
+    """The device evaluator's source run on the CPU."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty((len(x), 4))
+    st = lib().bfgBessel01Host(_ptr(x), len(x), _ptr(out))
+    if st != BFG_OK:
+        raise BfgError(st, "bessel01_host failed")
+    return out
+
+
+class Rng:
+    """The reference's seeded generator (rand.c:19-76), explicit state."""
+
+    def __init__(self, seed: int = 0):
+        self._s = _RngC()
+        self.seed(seed)
+
+    def seed(self, seed: int):
+        lib().bfgRngSeed(ctypes.byref(self._s), ctypes.c_uint64(seed))
+
+    def uniform(self, n: int) -> np.ndarray:
+        out = np.empty(n)
+        lib().bfgRngUniform(ctypes.byref(self._s), n, _ptr(out))
+        return out
+
+    def complex_randn(self, n: int) -> np.ndarray:
+        out = np.empty(n, dtype=np.complex128)
+        lib().bfgRngComplexRandn(ctypes.byref(self._s), n, _ptr(out))
+        return out
+
+
+def uniform_square_points(n: int, seed: int) -> np.ndarray:
+    """n points iid uniform in [-1,1]^2 from the seeded generator (x then y)."""
+    return (2.0 * Rng(seed).uniform(2 * n) - 1.0).reshape(n, 2)
+
+
+def curve_points(kind: str, n: int, a: float = 3.0, b: float = 2.0, amp: float = 0.5,
+                 lobes: int = 5) -> np.ndarray:
+    """Points equispaced in the curve parameter, theta_i = (2 pi / n) i."""
+    theta = (6.283185307179586 / n) * np.arange(n, dtype=np.float64)
+    if kind == "circle":
+        return np.stack([a * np.cos(theta), a * np.sin(theta)], axis=1)
+    if kind == "ellipse":
+        return np.stack([a * np.cos(theta), b * np.sin(theta)], axis=1)
+    if kind == "star":
+        r = a + amp * np.cos(lobes * theta)
+        return np.stack([r * np.cos(theta), r * np.sin(theta)], axis=1)
+    raise ValueError(kind)

@@ -1,0 +1,849 @@
+// C-ABI layer of libbfg.so (declarations and contracts in include/bfg.h).
+#include "../../include/bfg.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "bfg_kernels.cuh"
+#include "bfg_plan.hpp"
+#include "hankel.cuh"
+
+struct bfgContext_s {
+  int device = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string lastError;
+};
+
+namespace {
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes) return cudaSuccess;
+    release();
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    else p = nullptr;
+    return e;
+  }
+  template <typename T> T *as() const { return static_cast<T *>(p); }
+};
+
+struct BfgError {
+  bfgStatus status;
+  std::string msg;
+};
+
+void ck(cudaError_t e, char const *what) {
+  if (e != cudaSuccess)
+    throw BfgError{BFG_ERROR_CUDA, std::string(what) + ": " + cudaGetErrorString(e)};
+}
+
+template <typename T>
+void upload(DevBuf &buf, std::vector<T> const &v, cudaStream_t s, char const *what) {
+  size_t n = std::max<size_t>(1, v.size()) * sizeof(T);
+  ck(buf.ensure(n), what);
+  if (!v.empty())
+    ck(cudaMemcpyAsync(buf.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s), what);
+}
+
+}  // namespace
+
+struct bfgFac_s {
+  bfgContext ctx = nullptr;
+  bfgHelm2 helm{};
+  bfgFacOptions opts{};
+  bfg::Plan plan;
+  bfg::ApplyProgram prog;
+  bfgFacStats stats{};
+  // device data
+  DevBuf srcPts, tgtPts;            // x, y, nx, ny planes (tree order)
+  bool srcHasNormals = false, tgtHasNormals = false;
+  DevBuf arena64, arena32;
+  bool arena32Ready = false;
+  DevBuf srcPerm, tgtPerm;
+  DevBuf items, contribs, rowSeg, segStart, segContrib0, segBase;
+  DevBuf ws, xbuf;
+  DevBuf hx128, hy128, hx64, hy64;  // staging of the host-operand apply
+  std::vector<int64_t> stageItem0;
+};
+
+namespace {
+
+bfgStatus fail(bfgContext ctx, bfgStatus st, std::string const &msg) {
+  if (ctx) ctx->lastError = msg;
+  return st;
+}
+
+template <typename F>
+bfgStatus guarded(bfgContext ctx, F &&f) {
+  try {
+    if (ctx) {
+      int cur = -1;
+      if (cudaGetDevice(&cur) == cudaSuccess && cur != ctx->device) cudaSetDevice(ctx->device);
+    }
+    return f();
+  } catch (BfgError const &e) {
+    return fail(ctx, e.status, e.msg);
+  } catch (std::bad_alloc const &) {
+    return fail(ctx, BFG_ERROR_MEMORY, "host allocation failed");
+  } catch (std::exception const &e) {
+    return fail(ctx, BFG_ERROR_RUNTIME, e.what());
+  }
+}
+
+bfg::PointsDev pointsView(DevBuf const &b, int64_t n, bool normals) {
+  bfg::PointsDev p;
+  double const *base = b.as<double>();
+  p.x = base;
+  p.y = base + n;
+  if (normals) {
+    p.nx = base + 2 * n;
+    p.ny = base + 3 * n;
+  }
+  return p;
+}
+
+void uploadTreePoints(DevBuf &buf, double const *xy, double const *nrm, int64_t n,
+                      std::vector<int64_t> const &perm, cudaStream_t s) {
+  std::vector<double> h((size_t)(nrm ? 4 : 2) * n);
+  for (int64_t i = 0; i < n; ++i) {
+    int64_t o = perm[(size_t)i];
+    h[(size_t)i] = xy[2 * o];
+    h[(size_t)(n + i)] = xy[2 * o + 1];
+    if (nrm) {
+      h[(size_t)(2 * n + i)] = nrm[2 * o];
+      h[(size_t)(3 * n + i)] = nrm[2 * o + 1];
+    }
+  }
+  upload(buf, h, s, "upload points");
+}
+
+bfg::KernelParams kernelParams(bfgHelm2 const &h, int32_t layerPot) {
+  bfg::KernelParams kp{};
+  kp.k = h.k;
+  kp.layerPot = layerPot;
+  kp.alphaRe = h.alphaRe;
+  kp.alphaIm = h.alphaIm;
+  kp.betaRe = h.betaRe;
+  kp.betaIm = h.betaIm;
+  return kp;
+}
+
+int32_t proxyLayerPot(int32_t lp) {
+  // BF_PROXY_LAYER_POT (layer_pot.h:87-93)
+  switch (lp) {
+    case bfg::kLpSingle: return bfg::kLpSingle;
+    case bfg::kLpPvDouble: return bfg::kLpPvDouble;
+    case bfg::kLpPvNormalDerivSingle: return bfg::kLpSingle;
+    case bfg::kLpCombinedField: return bfg::kLpCombinedField;
+    default: return 0;
+  }
+}
+
+bool validLayerPot(int32_t lp) {
+  return lp == 1 || lp == 2 || lp == 3 || lp == 5;
+}
+
+bfg::FillDesc toDesc(bfg::Block const &b) {
+  bfg::FillDesc d{};
+  d.kind = b.kind;
+  d.m = b.m;
+  d.n = b.n;
+  d.arenaOff = b.arenaOff;
+  d.s0 = b.s0;
+  d.t0 = b.t0;
+  d.corig[0] = b.corig.cx; d.corig[1] = b.corig.cy; d.corig[2] = b.corig.r;
+  d.ceq[0] = b.ceq.cx; d.ceq[1] = b.ceq.cy; d.ceq[2] = b.ceq.r;
+  d.cchk[0] = b.cchk.cx; d.cchk[1] = b.cchk.cy; d.cchk[2] = b.cchk.r;
+  return d;
+}
+
+constexpr int64_t kSmemLimit = 220 * 1024;
+constexpr int64_t kScratchBudgetEntries = (int64_t)1 << 27;   // 2 GiB of complex128
+
+void factorize(bfgFac f) {
+  cudaStream_t s = f->ctx->stream;
+  bfg::Plan &plan = f->plan;
+  int64_t const nSrc = (int64_t)plan.src.perm.size(), nTgt = (int64_t)plan.tgt.perm.size();
+  (void)nTgt;
+  bfg::PointsDev src = pointsView(f->srcPts, nSrc, f->srcHasNormals);
+  bfg::PointsDev tgt = pointsView(f->tgtPts, (int64_t)plan.tgt.perm.size(), f->tgtHasNormals);
+
+  ck(f->arena64.ensure(std::max<int64_t>(1, plan.arenaEntries) * sizeof(double2)), "arena");
+
+  std::vector<bfg::FillDesc> fill, reSmall, reLarge, reGlobal;
+  int32_t maxProxyN = 1;
+  int64_t maxRank = 0;
+  for (auto const &b : plan.blocks) {
+    bfg::FillDesc d = toDesc(b);
+    if (b.kind == bfg::kLast || b.kind == bfg::kDense) {
+      fill.push_back(d);
+      if (b.kind == bfg::kLast) maxProxyN = std::max(maxProxyN, b.n);
+      if (b.kind == bfg::kLast) maxRank = std::max<int64_t>(maxRank, b.n);
+    } else {
+      maxRank = std::max<int64_t>(maxRank, b.m);
+      int64_t smem = bfg::reexpansionSmemBytes(b.m, b.n);
+      if (smem <= kSmemLimit) {
+        if (b.m <= 16) reSmall.push_back(d);
+        else reLarge.push_back(d);
+      } else {
+        reGlobal.push_back(d);
+      }
+    }
+  }
+  if (maxProxyN > 6000) throw BfgError{BFG_ERROR_NOT_IMPLEMENTED, "rank above 6000"};
+
+  DevBuf status, dFill, dSmall, dLarge, dGlobal, dScratchOff, scratch;
+  ck(status.ensure(sizeof(int32_t)), "status");
+  ck(cudaMemsetAsync(status.p, 0, sizeof(int32_t), s), "status");
+
+  cudaEvent_t e0, e1;
+  ck(cudaEventCreate(&e0), "event");
+  ck(cudaEventCreate(&e1), "event");
+  ck(cudaEventRecord(e0, s), "event");
+
+  bfg::KernelParams kpTrue = kernelParams(f->helm, f->helm.layerPot);
+  bfg::KernelParams kpProxy = kernelParams(f->helm, proxyLayerPot(f->helm.layerPot));
+  double2 *arena = f->arena64.as<double2>();
+  int32_t *st = status.as<int32_t>();
+
+  upload(dFill, fill, s, "descriptors");
+  ck(bfg::launchFillBlocks(dFill.as<bfg::FillDesc>(), (int32_t)fill.size(), src, tgt, kpTrue,
+                           arena, maxProxyN, st, s),
+     "fill kernel");
+
+  auto maxSmem = [](std::vector<bfg::FillDesc> const &v) {
+    int64_t m = 0;
+    for (auto const &d : v) m = std::max(m, bfg::reexpansionSmemBytes(d.m, d.n));
+    return (int32_t)m;
+  };
+  upload(dSmall, reSmall, s, "descriptors");
+  ck(bfg::launchReexpansion(dSmall.as<bfg::FillDesc>(), (int32_t)reSmall.size(), src, kpProxy,
+                            f->opts.pinvCut, f->opts.pinvTol, arena, nullptr, nullptr, st, true,
+                            maxSmem(reSmall), 256, s),
+     "re-expansion kernel");
+  upload(dLarge, reLarge, s, "descriptors");
+  ck(bfg::launchReexpansion(dLarge.as<bfg::FillDesc>(), (int32_t)reLarge.size(), src, kpProxy,
+                            f->opts.pinvCut, f->opts.pinvTol, arena, nullptr, nullptr, st, true,
+                            maxSmem(reLarge), 512, s),
+     "re-expansion kernel");
+
+  // blocks too large for shared memory: working matrices in global scratch,
+  // in batches bounded by the scratch budget
+  size_t i0 = 0;
+  while (i0 < reGlobal.size()) {
+    std::vector<int64_t> offs;
+    int64_t total = 0;
+    size_t i1 = i0;
+    int32_t geoBytes = 0;
+    while (i1 < reGlobal.size()) {
+      int64_t e = bfg::reexpansionScratchEntries(reGlobal[i1].m, reGlobal[i1].n);
+      if (i1 > i0 && total + e > kScratchBudgetEntries) break;
+      offs.push_back(total);
+      total += e;
+      geoBytes = std::max<int32_t>(
+          geoBytes, (int32_t)(8 * (7 * (int64_t)reGlobal[i1].m + 4 * (int64_t)reGlobal[i1].n)));
+      ++i1;
+    }
+    if (geoBytes > kSmemLimit) throw BfgError{BFG_ERROR_NOT_IMPLEMENTED, "block geometry exceeds shared memory"};
+    std::vector<bfg::FillDesc> batch(reGlobal.begin() + (long)i0, reGlobal.begin() + (long)i1);
+    ck(scratch.ensure((size_t)total * sizeof(double2)), "re-expansion scratch");
+    upload(dGlobal, batch, s, "descriptors");
+    upload(dScratchOff, offs, s, "descriptors");
+    ck(bfg::launchReexpansion(dGlobal.as<bfg::FillDesc>(), (int32_t)batch.size(), src, kpProxy,
+                              f->opts.pinvCut, f->opts.pinvTol, arena, scratch.as<double2>(),
+                              dScratchOff.as<int64_t>(), st, false, geoBytes, 512, s),
+       "re-expansion kernel (global)");
+    // the batch's descriptors and offsets must stay alive until it ran
+    ck(cudaStreamSynchronize(s), "re-expansion");
+    i0 = i1;
+  }
+  ck(cudaEventRecord(e1, s), "event");
+  ck(cudaStreamSynchronize(s), "factorization");
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  int32_t hst = 0;
+  ck(cudaMemcpy(&hst, status.p, sizeof hst, cudaMemcpyDeviceToHost), "status");
+  if (hst & bfg::kStatusBadDescriptor) throw BfgError{BFG_ERROR_RUNTIME, "bad block descriptor"};
+
+  f->stats.factorMs = ms;
+  f->stats.maxRank = maxRank;
+  f->stats.jacobiNotConverged = (hst & bfg::kStatusJacobiNotConverged) ? 1 : 0;
+}
+
+void buildApply(bfgFac f) {
+  cudaStream_t s = f->ctx->stream;
+  bfg::makeApplyProgram(f->plan, f->prog);
+  bfg::ApplyProgram const &p = f->prog;
+  upload(f->items, p.items, s, "apply program");
+  upload(f->contribs, p.contribs, s, "apply program");
+  upload(f->rowSeg, p.rowSeg, s, "apply program");
+  upload(f->segStart, p.segStart, s, "apply program");
+  upload(f->segContrib0, p.segContrib0, s, "apply program");
+  upload(f->segBase, p.segBase, s, "apply program");
+  f->stageItem0 = p.stageItem0;
+  ck(cudaStreamSynchronize(s), "apply program");
+}
+
+void fillStats(bfgFac f) {
+  bfgFacStats &st = f->stats;
+  st.numRows = (int64_t)f->plan.tgt.perm.size();
+  st.numCols = (int64_t)f->plan.src.perm.size();
+  st.numBlocks = (int64_t)f->plan.blocks.size();
+  st.numFirst = st.numMiddle = st.numLast = st.numDense = 0;
+  for (auto const &b : f->plan.blocks) {
+    if (b.kind == bfg::kFirst) ++st.numFirst;
+    else if (b.kind == bfg::kMiddle) ++st.numMiddle;
+    else if (b.kind == bfg::kLast) ++st.numLast;
+    else ++st.numDense;
+  }
+  st.numProducts = (int64_t)f->plan.products.size();
+  st.arenaEntries = f->plan.arenaEntries;
+  st.numStages = (int64_t)f->stageItem0.size() - 1;
+  st.numItems = (int64_t)f->prog.items.size();
+  st.flopsPerRhs = f->prog.flopsPerRhs;
+}
+
+template <typename T2>
+void runApply(bfgFac f, T2 const *arena, T2 const *X, int64_t ldx, int64_t R, T2 *Y,
+              int64_t ldy, uint32_t flags, std::vector<cudaEvent_t> *events) {
+  cudaStream_t s = f->ctx->stream;
+  bfg::ApplyProgram const &p = f->prog;
+  ck(f->ws.ensure((size_t)std::max<int64_t>(1, p.wsRows) * R * sizeof(T2)), "workspace");
+  T2 *W = f->ws.as<T2>();
+  T2 const *Xt = X;
+  int64_t ldxt = ldx;
+  size_t ev = 0;
+  auto mark = [&]() {
+    if (events) ck(cudaEventRecord((*events)[ev++], s), "event");
+  };
+  mark();
+  if (flags & BFG_APPLY_ORIGINAL_ORDER) {
+    ck(f->xbuf.ensure((size_t)p.numCols * R * sizeof(T2)), "gather buffer");
+    ck(bfg::launchGatherRows<T2>(X, ldx, f->srcPerm.as<int64_t>(), p.numCols, R,
+                                 f->xbuf.as<T2>(), s),
+       "gather");
+    Xt = f->xbuf.as<T2>();
+    ldxt = R;
+    mark();
+  }
+  size_t const nStages = f->stageItem0.size() - 1;
+  for (size_t st = 0; st < nStages; ++st) {
+    int64_t a = f->stageItem0[st], b = f->stageItem0[st + 1];
+    ck(bfg::launchApplyStage<T2>(f->items.as<bfg::ApplyItem>() + a, b - a,
+                                 f->contribs.as<bfg::ApplyContrib>(), arena, Xt, ldxt, W, R, s),
+       "apply stage");
+    mark();
+  }
+  ck(bfg::launchApplyReduce<T2>(f->rowSeg.as<int32_t>(), f->segStart.as<int64_t>(),
+                                f->segContrib0.as<int64_t>(), f->segBase.as<int64_t>(), W, R, Y,
+                                ldy, p.numRows,
+                                (flags & BFG_APPLY_ORIGINAL_ORDER) ? f->tgtPerm.as<int64_t>()
+                                                                  : nullptr,
+                                s),
+     "apply reduce");
+  mark();
+}
+
+size_t numApplyLaunches(bfgFac f, uint32_t flags) {
+  return (f->stageItem0.size() - 1) + 1 + ((flags & BFG_APPLY_ORIGINAL_ORDER) ? 1 : 0);
+}
+
+void ensureArena32(bfgFac f) {
+  if (f->arena32Ready) return;
+  int64_t n = std::max<int64_t>(1, f->plan.arenaEntries);
+  ck(f->arena32.ensure((size_t)n * sizeof(float2)), "FP32 arena");
+  ck(bfg::launchArenaToF32(f->arena64.as<double2>(), f->arena32.as<float2>(), f->plan.arenaEntries,
+                           f->ctx->stream),
+     "FP32 arena");
+  f->arena32Ready = true;
+}
+
+bfgStatus applyDispatch(bfgFac f, bfgPrecision prec, void const *X, int64_t ldx, int64_t R,
+                        void *Y, int64_t ldy, uint32_t flags, std::vector<cudaEvent_t> *ev) {
+  if (!X || !Y || R < 1 || ldx < R || ldy < R)
+    return fail(f->ctx, BFG_ERROR_INVALID_ARGUMENTS, "apply: bad operand pointers or shapes");
+  if (flags & ~BFG_APPLY_ORIGINAL_ORDER)
+    return fail(f->ctx, BFG_ERROR_INVALID_ARGUMENTS, "apply: unknown flags");
+  if (prec == BFG_PRECISION_FP64) {
+    runApply<double2>(f, f->arena64.as<double2>(), static_cast<double2 const *>(X), ldx, R,
+                      static_cast<double2 *>(Y), ldy, flags, ev);
+  } else if (prec == BFG_PRECISION_FP32) {
+    ensureArena32(f);
+    runApply<float2>(f, f->arena32.as<float2>(), static_cast<float2 const *>(X), ldx, R,
+                     static_cast<float2 *>(Y), ldy, flags, ev);
+  } else {
+    return fail(f->ctx, BFG_ERROR_NOT_IMPLEMENTED, "apply: unknown precision");
+  }
+  return BFG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+bfgStatus bfgContextCreate(int32_t device, bfgContext *out) {
+  if (!out) return BFG_ERROR_INVALID_ARGUMENTS;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return BFG_ERROR_CUDA;
+  if (device < 0 || device >= count) return BFG_ERROR_INVALID_ARGUMENTS;
+  auto *ctx = new (std::nothrow) bfgContext_s;
+  if (!ctx) return BFG_ERROR_MEMORY;
+  ctx->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return BFG_ERROR_CUDA;
+  }
+  ctx->stream = ctx->own;
+  *out = ctx;
+  return BFG_OK;
+}
+
+bfgStatus bfgContextDestroy(bfgContext ctx) {
+  if (!ctx) return BFG_ERROR_INVALID_ARGUMENTS;
+  if (ctx->own) {
+    cudaStreamSynchronize(ctx->own);
+    cudaStreamDestroy(ctx->own);
+  }
+  delete ctx;
+  return BFG_OK;
+}
+
+bfgStatus bfgContextSetStream(bfgContext ctx, void *stream) {
+  if (!ctx) return BFG_ERROR_INVALID_ARGUMENTS;
+  ctx->stream = static_cast<cudaStream_t>(stream);
+  return BFG_OK;
+}
+
+bfgStatus bfgContextGetStream(bfgContext ctx, void **stream) {
+  if (!ctx || !stream) return BFG_ERROR_INVALID_ARGUMENTS;
+  *stream = ctx->stream;
+  return BFG_OK;
+}
+
+bfgStatus bfgContextSynchronize(bfgContext ctx) {
+  if (!ctx) return BFG_ERROR_INVALID_ARGUMENTS;
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return fail(ctx, BFG_ERROR_CUDA, cudaGetErrorString(e));
+  return BFG_OK;
+}
+
+char const *bfgGetErrorString(bfgContext ctx) {
+  return ctx ? ctx->lastError.c_str() : "no context";
+}
+
+void bfgFacOptionsDefault(bfgFacOptions *o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof *o);
+  o->leafSize = 1;
+  o->rankEps = 1e-15;
+  o->pinvCut = 0;
+  o->pinvTol = 0.0;
+}
+
+bfgStatus bfgFacHelm2MakeMultilevel(bfgContext ctx, bfgHelm2 const *helm, double const *srcXy,
+                                    double const *srcNormals, int64_t numSrc,
+                                    double const *tgtXy, double const *tgtNormals,
+                                    int64_t numTgt, bfgFacOptions const *opts, bfgFac *out) {
+  if (!ctx) return BFG_ERROR_INVALID_ARGUMENTS;
+  return guarded(ctx, [&]() -> bfgStatus {
+    if (!helm || !srcXy || !tgtXy || !out || numSrc < 1 || numTgt < 1)
+      return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "make: null argument or empty point set");
+    *out = nullptr;
+    if (!(helm->k > 0) || !validLayerPot(helm->layerPot))
+      return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "make: k must be > 0 and the layer potential known");
+    bool const needSrcN = helm->layerPot == bfg::kLpPvDouble ||
+                          helm->layerPot == bfg::kLpCombinedField;
+    bool const needTgtN = helm->layerPot == bfg::kLpPvNormalDerivSingle;
+    if ((needSrcN && !srcNormals) || (needTgtN && !tgtNormals))
+      return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "make: this layer potential needs normals");
+    bfgFacOptions o;
+    bfgFacOptionsDefault(&o);
+    if (opts) o = *opts;
+    if (o.leafSize < 1 || !(o.rankEps > 0 && o.rankEps < 1) || (o.pinvCut != 0 && o.pinvCut != 1) ||
+        (o.pinvCut == 1 && !(o.pinvTol > 0 && o.pinvTol < 1)))
+      return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "make: bad options");
+    for (int64_t i = 0; i < 2 * numSrc; ++i)
+      if (!std::isfinite(srcXy[i])) return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "make: non-finite source point");
+    for (int64_t i = 0; i < 2 * numTgt; ++i)
+      if (!std::isfinite(tgtXy[i])) return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "make: non-finite target point");
+
+    auto *f = new bfgFac_s;
+    f->ctx = ctx;
+    f->helm = *helm;
+    f->opts = o;
+    try {
+      bfg::PlanParams pp;
+      pp.k = helm->k;
+      pp.leafSize = o.leafSize;
+      pp.rankEps = o.rankEps;
+      bfg::makePlan(f->plan, pp, srcXy, numSrc, tgtXy, numTgt);
+      cudaStream_t s = ctx->stream;
+      f->srcHasNormals = srcNormals != nullptr;
+      f->tgtHasNormals = tgtNormals != nullptr;
+      uploadTreePoints(f->srcPts, srcXy, srcNormals, numSrc, f->plan.src.perm, s);
+      uploadTreePoints(f->tgtPts, tgtXy, tgtNormals, numTgt, f->plan.tgt.perm, s);
+      upload(f->srcPerm, f->plan.src.perm, s, "perm");
+      upload(f->tgtPerm, f->plan.tgt.perm, s, "perm");
+      factorize(f);
+      buildApply(f);
+      fillStats(f);
+    } catch (std::runtime_error const &e) {
+      delete f;
+      return fail(ctx, BFG_ERROR_RUNTIME, std::string("make: ") + e.what());
+    } catch (...) {
+      delete f;
+      throw;
+    }
+    *out = f;
+    return BFG_OK;
+  });
+}
+
+bfgStatus bfgFacDestroy(bfgFac f) {
+  if (!f) return BFG_ERROR_INVALID_ARGUMENTS;
+  cudaStreamSynchronize(f->ctx->stream);
+  delete f;
+  return BFG_OK;
+}
+
+bfgStatus bfgFacGetShape(bfgFac f, int64_t *rows, int64_t *cols) {
+  if (!f || !rows || !cols) return BFG_ERROR_INVALID_ARGUMENTS;
+  *rows = (int64_t)f->plan.tgt.perm.size();
+  *cols = (int64_t)f->plan.src.perm.size();
+  return BFG_OK;
+}
+
+bfgStatus bfgFacGetPerms(bfgFac f, int64_t *srcPerm, int64_t *tgtPerm) {
+  if (!f) return BFG_ERROR_INVALID_ARGUMENTS;
+  if (srcPerm) std::copy(f->plan.src.perm.begin(), f->plan.src.perm.end(), srcPerm);
+  if (tgtPerm) std::copy(f->plan.tgt.perm.begin(), f->plan.tgt.perm.end(), tgtPerm);
+  return BFG_OK;
+}
+
+bfgStatus bfgFacNumBytes(bfgFac f, int64_t *bytes) {
+  if (!f || !bytes) return BFG_ERROR_INVALID_ARGUMENTS;
+  *bytes = f->plan.arenaEntries * 16;
+  return BFG_OK;
+}
+
+bfgStatus bfgFacGetStats(bfgFac f, bfgFacStats *st) {
+  if (!f || !st) return BFG_ERROR_INVALID_ARGUMENTS;
+  *st = f->stats;
+  return BFG_OK;
+}
+
+bfgStatus bfgFacDescribe(bfgFac f, char *buf, int64_t cap, int64_t *len) {
+  if (!f || !len) return BFG_ERROR_INVALID_ARGUMENTS;
+  return guarded(f->ctx, [&]() -> bfgStatus {
+    std::string t = f->plan.text();
+    *len = (int64_t)t.size();
+    if (buf && cap > 0) {
+      int64_t n = std::min<int64_t>(cap - 1, (int64_t)t.size());
+      std::memcpy(buf, t.data(), (size_t)n);
+      buf[n] = 0;
+      if (cap <= (int64_t)t.size()) return fail(f->ctx, BFG_ERROR_OUT_OF_RANGE, "describe: buffer too small");
+    }
+    return BFG_OK;
+  });
+}
+
+bfgStatus bfgFacCopyBlocks(bfgFac f, double *entries, int64_t capEntries, int64_t *table,
+                           int64_t capBlocks) {
+  if (!f) return BFG_ERROR_INVALID_ARGUMENTS;
+  return guarded(f->ctx, [&]() -> bfgStatus {
+    if (entries) {
+      if (capEntries < f->plan.arenaEntries)
+        return fail(f->ctx, BFG_ERROR_OUT_OF_RANGE, "copy blocks: entry buffer too small");
+      ck(cudaStreamSynchronize(f->ctx->stream), "sync");
+      ck(cudaMemcpy(entries, f->arena64.p, (size_t)f->plan.arenaEntries * 16, cudaMemcpyDeviceToHost),
+         "copy blocks");
+    }
+    if (table) {
+      if (capBlocks < (int64_t)f->plan.blocks.size())
+        return fail(f->ctx, BFG_ERROR_OUT_OF_RANGE, "copy blocks: table too small");
+      for (size_t i = 0; i < f->plan.blockOrder.size(); ++i) {
+        auto const &b = f->plan.blocks[f->plan.blockOrder[i]];
+        table[4 * i] = b.kind;
+        table[4 * i + 1] = b.m;
+        table[4 * i + 2] = b.n;
+        table[4 * i + 3] = b.arenaOff;
+      }
+    }
+    return BFG_OK;
+  });
+}
+
+bfgStatus bfgFacApply(bfgFac f, bfgPrecision prec, void const *X, int64_t ldx, int64_t R,
+                      void *Y, int64_t ldy, uint32_t flags) {
+  if (!f) return BFG_ERROR_INVALID_ARGUMENTS;
+  return guarded(f->ctx, [&]() { return applyDispatch(f, prec, X, ldx, R, Y, ldy, flags, nullptr); });
+}
+
+bfgStatus bfgFacApplyTimed(bfgFac f, bfgPrecision prec, void const *X, int64_t ldx, int64_t R,
+                           void *Y, int64_t ldy, uint32_t flags, float *ms, int32_t cap,
+                           int32_t *numLaunches) {
+  if (!f || !numLaunches) return BFG_ERROR_INVALID_ARGUMENTS;
+  return guarded(f->ctx, [&]() -> bfgStatus {
+    size_t const n = numApplyLaunches(f, flags);
+    *numLaunches = (int32_t)n;
+    if (!ms || cap < (int32_t)n) return fail(f->ctx, BFG_ERROR_OUT_OF_RANGE, "timed apply: buffer too small");
+    if (prec == BFG_PRECISION_FP32) ensureArena32(f);
+    std::vector<cudaEvent_t> ev(n + 1);
+    for (auto &e : ev) ck(cudaEventCreate(&e), "event");
+    bfgStatus st = applyDispatch(f, prec, X, ldx, R, Y, ldy, flags, &ev);
+    if (st == BFG_OK) {
+      ck(cudaEventSynchronize(ev[n]), "event");
+      for (size_t i = 0; i < n; ++i) cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    return st;
+  });
+}
+
+bfgStatus bfgFacGetLaunchInfo(bfgFac f, uint32_t flags, int64_t *info, int32_t cap,
+                              int32_t *numLaunches) {
+  if (!f || !numLaunches) return BFG_ERROR_INVALID_ARGUMENTS;
+  size_t const n = numApplyLaunches(f, flags);
+  *numLaunches = (int32_t)n;
+  if (!info || cap < (int32_t)n) return fail(f->ctx, BFG_ERROR_OUT_OF_RANGE, "launch info: buffer too small");
+  bfg::ApplyProgram const &p = f->prog;
+  size_t k = 0;
+  if (flags & BFG_APPLY_ORIGINAL_ORDER) {
+    info[3 * k] = 0;
+    info[3 * k + 1] = p.numCols;
+    info[3 * k + 2] = p.numCols;
+    ++k;
+  }
+  for (size_t s = 0; s + 1 < f->stageItem0.size(); ++s, ++k) {
+    info[3 * k] = p.stageEntries[s];
+    info[3 * k + 1] = p.stageRowsIn[s];
+    info[3 * k + 2] = p.stageRowsOut[s];
+  }
+  info[3 * k] = 0;
+  info[3 * k + 1] = p.sumRows;
+  info[3 * k + 2] = p.numRows;
+  return BFG_OK;
+}
+
+bfgStatus bfgFacApplyHost(bfgFac f, bfgPrecision prec, double const *X, int64_t ldx, int64_t R,
+                          double *Y, int64_t ldy, uint32_t flags) {
+  if (!f) return BFG_ERROR_INVALID_ARGUMENTS;
+  return guarded(f->ctx, [&]() -> bfgStatus {
+    if (!X || !Y || R < 1 || ldx < R || ldy < R)
+      return fail(f->ctx, BFG_ERROR_INVALID_ARGUMENTS, "apply: bad operand pointers or shapes");
+    cudaStream_t s = f->ctx->stream;
+    int64_t const nr = f->prog.numRows, nc = f->prog.numCols;
+    // complex128 staging on the device (the host operands are complex128
+    // whatever the arithmetic); the buffers persist across calls
+    ck(f->hx128.ensure((size_t)nc * R * 16), "apply buffers");
+    ck(f->hy128.ensure((size_t)nr * R * 16), "apply buffers");
+    ck(cudaMemcpy2DAsync(f->hx128.p, (size_t)R * 16, X, (size_t)ldx * 16, (size_t)R * 16,
+                         (size_t)nc, cudaMemcpyHostToDevice, s),
+       "copy X");
+    if (prec == BFG_PRECISION_FP64) {
+      bfgStatus st = applyDispatch(f, prec, f->hx128.p, R, R, f->hy128.p, R, flags, nullptr);
+      if (st != BFG_OK) return st;
+    } else if (prec == BFG_PRECISION_FP32) {
+      ck(f->hx64.ensure((size_t)nc * R * 8), "apply buffers");
+      ck(f->hy64.ensure((size_t)nr * R * 8), "apply buffers");
+      ck(bfg::launchC128ToC64(f->hx128.as<double2>(), R, nc, R, f->hx64.as<float2>(), R, s),
+         "convert X");
+      bfgStatus st = applyDispatch(f, prec, f->hx64.p, R, R, f->hy64.p, R, flags, nullptr);
+      if (st != BFG_OK) return st;
+      ck(bfg::launchC64ToC128(f->hy64.as<float2>(), R, nr, R, f->hy128.as<double2>(), R, s),
+         "convert Y");
+    } else {
+      return fail(f->ctx, BFG_ERROR_NOT_IMPLEMENTED, "apply: unknown precision");
+    }
+    ck(cudaMemcpy2DAsync(Y, (size_t)ldy * 16, f->hy128.p, (size_t)R * 16, (size_t)R * 16,
+                         (size_t)nr, cudaMemcpyDeviceToHost, s),
+       "copy Y");
+    ck(cudaStreamSynchronize(s), "apply");
+    return BFG_OK;
+  });
+}
+
+bfgStatus bfgFacDenseRows(bfgFac f, int64_t const *rows, int64_t nSel, void const *X, int64_t ldx,
+                          int64_t R, void *out, int64_t ldo) {
+  if (!f) return BFG_ERROR_INVALID_ARGUMENTS;
+  return guarded(f->ctx, [&]() -> bfgStatus {
+    if (!rows || !X || !out || nSel < 0 || R < 1 || ldx < R || ldo < R)
+      return fail(f->ctx, BFG_ERROR_INVALID_ARGUMENTS, "dense rows: bad arguments");
+    int64_t const nr = f->prog.numRows, nc = f->prog.numCols;
+    std::vector<int64_t> r(rows, rows + nSel);
+    for (int64_t v : r)
+      if (v < 0 || v >= nr) return fail(f->ctx, BFG_ERROR_OUT_OF_RANGE, "dense rows: row out of range");
+    DevBuf dr;
+    upload(dr, r, f->ctx->stream, "rows");
+    bfg::KernelParams kp = kernelParams(f->helm, f->helm.layerPot);
+    ck(bfg::launchDenseRows(pointsView(f->srcPts, nc, f->srcHasNormals), nc,
+                            pointsView(f->tgtPts, nr, f->tgtHasNormals), dr.as<int64_t>(), nSel,
+                            kp, static_cast<double2 const *>(X), ldx, R,
+                            static_cast<double2 *>(out), ldo, f->ctx->stream),
+       "dense rows");
+    ck(cudaStreamSynchronize(f->ctx->stream), "dense rows");
+    return BFG_OK;
+  });
+}
+
+bfgStatus bfgHelm2KernelMatrix(bfgContext ctx, bfgHelm2 const *helm, double const *srcXy,
+                               double const *srcNormals, int64_t n, double const *tgtXy,
+                               double const *tgtNormals, int64_t m, double *out) {
+  if (!ctx) return BFG_ERROR_INVALID_ARGUMENTS;
+  return guarded(ctx, [&]() -> bfgStatus {
+    if (!helm || !srcXy || !tgtXy || !out || n < 0 || m < 0 || !validLayerPot(helm->layerPot))
+      return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "kernel matrix: bad arguments");
+    bool const needSrcN = helm->layerPot == bfg::kLpPvDouble ||
+                          helm->layerPot == bfg::kLpCombinedField;
+    bool const needTgtN = helm->layerPot == bfg::kLpPvNormalDerivSingle;
+    if ((needSrcN && !srcNormals) || (needTgtN && !tgtNormals))
+      return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "kernel matrix: normals needed");
+    cudaStream_t s = ctx->stream;
+    std::vector<int64_t> idS(n), idT(m);
+    for (int64_t i = 0; i < n; ++i) idS[i] = i;
+    for (int64_t i = 0; i < m; ++i) idT[i] = i;
+    DevBuf ds, dt, dout;
+    uploadTreePoints(ds, srcXy, srcNormals, n, idS, s);
+    uploadTreePoints(dt, tgtXy, tgtNormals, m, idT, s);
+    ck(dout.ensure((size_t)std::max<int64_t>(1, m * n) * 16), "kernel matrix");
+    ck(bfg::launchKernelMatrix(pointsView(ds, n, srcNormals != nullptr), n,
+                               pointsView(dt, m, tgtNormals != nullptr), m,
+                               kernelParams(*helm, helm->layerPot), dout.as<double2>(), s),
+       "kernel matrix");
+    ck(cudaMemcpyAsync(out, dout.p, (size_t)m * n * 16, cudaMemcpyDeviceToHost, s), "kernel matrix");
+    ck(cudaStreamSynchronize(s), "kernel matrix");
+    return BFG_OK;
+  });
+}
+
+bfgStatus bfgBessel01(bfgContext ctx, double const *x, int64_t n, double *out) {
+  if (!ctx) return BFG_ERROR_INVALID_ARGUMENTS;
+  return guarded(ctx, [&]() -> bfgStatus {
+    if (!x || !out || n < 0) return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "bessel: bad arguments");
+    for (int64_t i = 0; i < n; ++i)
+      if (!(x[i] > 0) || !std::isfinite(x[i]))
+        return fail(ctx, BFG_ERROR_OUT_OF_RANGE, "bessel: arguments must be finite and > 0");
+    cudaStream_t s = ctx->stream;
+    DevBuf dx, dout;
+    ck(dx.ensure((size_t)std::max<int64_t>(1, n) * 8), "bessel");
+    ck(dout.ensure((size_t)std::max<int64_t>(1, n) * 32), "bessel");
+    ck(cudaMemcpyAsync(dx.p, x, (size_t)n * 8, cudaMemcpyHostToDevice, s), "bessel");
+    ck(bfg::launchBessel01(dx.as<double>(), n, dout.as<double>(), s), "bessel");
+    ck(cudaMemcpyAsync(out, dout.p, (size_t)n * 32, cudaMemcpyDeviceToHost, s), "bessel");
+    ck(cudaStreamSynchronize(s), "bessel");
+    return BFG_OK;
+  });
+}
+
+bfgStatus bfgPlanHelm2(double k, double const *srcXy, int64_t numSrc, double const *tgtXy,
+                       int64_t numTgt, bfgFacOptions const *opts, int64_t *srcPerm,
+                       int64_t *tgtPerm, char *buf, int64_t cap, int64_t *len) {
+  if (!srcXy || !tgtXy || numSrc < 1 || numTgt < 1 || !(k > 0)) return BFG_ERROR_INVALID_ARGUMENTS;
+  try {
+    bfgFacOptions o;
+    bfgFacOptionsDefault(&o);
+    if (opts) o = *opts;
+    if (o.leafSize < 1 || !(o.rankEps > 0 && o.rankEps < 1)) return BFG_ERROR_INVALID_ARGUMENTS;
+    bfg::PlanParams pp;
+    pp.k = k;
+    pp.leafSize = o.leafSize;
+    pp.rankEps = o.rankEps;
+    bfg::Plan plan;
+    bfg::makePlan(plan, pp, srcXy, numSrc, tgtXy, numTgt);
+    if (srcPerm) std::copy(plan.src.perm.begin(), plan.src.perm.end(), srcPerm);
+    if (tgtPerm) std::copy(plan.tgt.perm.begin(), plan.tgt.perm.end(), tgtPerm);
+    std::string t = plan.text();
+    if (len) *len = (int64_t)t.size();
+    if (buf && cap > 0) {
+      int64_t n = std::min<int64_t>(cap - 1, (int64_t)t.size());
+      std::memcpy(buf, t.data(), (size_t)n);
+      buf[n] = 0;
+      if (cap <= (int64_t)t.size()) return BFG_ERROR_OUT_OF_RANGE;
+    }
+    return BFG_OK;
+  } catch (std::bad_alloc const &) {
+    return BFG_ERROR_MEMORY;
+  } catch (std::exception const &) {
+    return BFG_ERROR_RUNTIME;
+  }
+}
+
+bfgStatus bfgBessel01Host(double const *x, int64_t n, double *out) {
+  if (!x || !out || n < 0) return BFG_ERROR_INVALID_ARGUMENTS;
+  for (int64_t i = 0; i < n; ++i) {
+    if (!(x[i] > 0) || !std::isfinite(x[i])) return BFG_ERROR_OUT_OF_RANGE;
+    bfg::Bessel01 b = bfg::bessel01<true>(x[i]);
+    out[4 * i] = b.j0;
+    out[4 * i + 1] = b.y0;
+    out[4 * i + 2] = b.j1;
+    out[4 * i + 3] = b.y1;
+  }
+  return BFG_OK;
+}
+
+// rand.c:19-76 with explicit state
+void bfgRngSeed(bfgRng *rng, uint64_t seed) {
+  uint64_t x = seed;
+  for (int i = 0; i < 4; ++i) {
+    uint64_t z = (x += 0x9e3779b97f4a7c15ULL);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    rng->s[i] = z ^ (z >> 31);
+  }
+}
+
+static uint64_t rngNext(bfgRng *rng) {
+  uint64_t *s = rng->s;
+  uint64_t const result = s[0] + s[3];
+  uint64_t const t = s[1] << 17;
+  s[2] ^= s[0];
+  s[3] ^= s[1];
+  s[1] ^= s[2];
+  s[0] ^= s[3];
+  s[2] ^= t;
+  s[3] = (s[3] << 45) | (s[3] >> 19);
+  return result;
+}
+
+double bfgRngUniform1(bfgRng *rng) { return (double)(rngNext(rng) >> 11) * 0x1.0p-53; }
+
+void bfgRngUniform(bfgRng *rng, int64_t n, double *out) {
+  for (int64_t i = 0; i < n; ++i) out[i] = bfgRngUniform1(rng);
+}
+
+void bfgRngComplexRandn(bfgRng *rng, int64_t n, double *x) {
+  // bfRealRandn on 2n reals (rand.c:50-76)
+  int64_t const m = 2 * n;
+  bfgRngUniform(rng, 2 * (m / 2), x);
+  double const twoPi = 6.283185307179586;
+  for (int64_t i = 0; i < m / 2; ++i) {
+    double mag = std::sqrt(-2 * std::log(x[2 * i]));
+    double theta = twoPi * x[2 * i + 1];
+    x[2 * i] = mag * std::cos(theta);
+    x[2 * i + 1] = mag * std::sin(theta);
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,101 @@
+// Kernel launchers shared between the C-ABI layer and the CUDA sources.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "bfg_plan.hpp"
+
+namespace bfg {
+
+// Layer potentials, numbered as the reference's BfLayerPotential
+// (layer_pot.h:52-65).
+enum LayerPot : int32_t {
+  kLpSingle = 1,
+  kLpPvDouble = 2,
+  kLpPvNormalDerivSingle = 3,
+  kLpCombinedField = 5,
+};
+
+struct KernelParams {
+  double k;
+  int32_t layerPot;        // layer potential of this fill
+  int32_t pad;
+  double alphaRe, alphaIm, betaRe, betaIm;
+};
+
+struct PointsDev {
+  double const *x = nullptr, *y = nullptr;    // tree order
+  double const *nx = nullptr, *ny = nullptr;  // unit normals or null
+};
+
+// status word bits written by the kernels
+enum : int32_t {
+  kStatusJacobiNotConverged = 1,
+  kStatusBadDescriptor = 2,
+};
+
+// Fills LAST and DENSE blocks (plain kernel evaluation).
+// maxProxyN bounds n over the LAST blocks of the launch (shared memory).
+cudaError_t launchFillBlocks(FillDesc const *descs, int32_t nDesc, PointsDev src,
+                             PointsDev tgt, KernelParams kp, double2 *arena,
+                             int32_t maxProxyN, int32_t *status, cudaStream_t stream);
+
+// Fills FIRST/MIDDLE blocks: proxy kernel matrices + pseudo-inverse
+// re-expansion.  `smem` selects the shared-memory variant (every block
+// must fit); otherwise `scratch` holds each CTA's working matrix at
+// scratchOff[cta] (complex entries).
+cudaError_t launchReexpansion(FillDesc const *descs, int32_t nDesc, PointsDev src,
+                              KernelParams kp, int32_t cutMode, double cutTol,
+                              double2 *arena, double2 *scratch,
+                              int64_t const *scratchOff, int32_t *status,
+                              bool smem, int32_t maxSmemBytes, int32_t threads,
+                              cudaStream_t stream);
+
+// Shared-memory bytes the re-expansion of an m x n block needs.
+int64_t reexpansionSmemBytes(int32_t m, int32_t n);
+int64_t reexpansionScratchEntries(int32_t m, int32_t n);
+
+// Dense kernel rows: out[s*ldo + r] = sum_j K(t_rows[s], src_j) x[j*ldx + r]
+cudaError_t launchDenseRows(PointsDev src, int64_t nSrc, PointsDev tgt,
+                            int64_t const *rows, int64_t nRows, KernelParams kp,
+                            double2 const *x, int64_t ldx, int64_t R, double2 *out,
+                            int64_t ldo, cudaStream_t stream);
+
+// Kernel matrix K(tgt_i, src_j), row-major m x n, points given directly.
+cudaError_t launchKernelMatrix(PointsDev src, int64_t n, PointsDev tgt, int64_t m,
+                               KernelParams kp, double2 *out, cudaStream_t stream);
+
+// H0, H1 at x[i]: out[4i..4i+3] = J0, Y0, J1, Y1
+cudaError_t launchBessel01(double const *x, int64_t n, double *out, cudaStream_t stream);
+
+// FP64 -> FP32 arena conversion (same layout)
+cudaError_t launchArenaToF32(double2 const *a64, float2 *a32, int64_t n, cudaStream_t stream);
+
+// complex128 <-> complex64 matrix conversion (row-major, leading dims)
+cudaError_t launchC128ToC64(double2 const *a, int64_t lda, int64_t rows, int64_t cols,
+                            float2 *b, int64_t ldb, cudaStream_t stream);
+cudaError_t launchC64ToC128(float2 const *a, int64_t lda, int64_t rows, int64_t cols,
+                            double2 *b, int64_t ldb, cudaStream_t stream);
+
+// Apply: one stage of items, element type T2 (double2 or float2).
+template <typename T2>
+cudaError_t launchApplyStage(ApplyItem const *items, int64_t nItems,
+                             ApplyContrib const *contribs, T2 const *arena,
+                             T2 const *X, int64_t ldx, T2 *W, int64_t R,
+                             cudaStream_t stream);
+
+template <typename T2>
+cudaError_t launchApplyReduce(int32_t const *rowSeg, int64_t const *segStart,
+                              int64_t const *segContrib0, int64_t const *segBase,
+                              T2 const *W, int64_t R, T2 *Y, int64_t ldy,
+                              int64_t nRows, int64_t const *outPerm,
+                              cudaStream_t stream);
+
+// X_tree[i] = X[perm[i]] (row gather, R columns)
+template <typename T2>
+cudaError_t launchGatherRows(T2 const *X, int64_t ldx, int64_t const *perm,
+                             int64_t nRows, int64_t R, T2 *out, cudaStream_t stream);
+
+}  // namespace bfg

@@ -1,0 +1,167 @@
+// Host-side structure of a butterfly factorization: quadtrees, the planner
+// that walks node pairs exactly like the reference's bfFacHelm2MakeMultilevel
+// (fac_helm2.c:551-1002), and the flat descriptor tables the GPU kernels
+// consume (block fill, batched re-expansion, staged apply).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace bfg {
+
+struct Circle {
+  double cx = 0, cy = 0, r = 0;
+};
+
+// Quadtree over a point set, built with the reference's split rule and sift
+// order (quadtree_node.c:123-306).  `perm[i]` is the original index of the
+// point at tree position i (BfTree.perm).
+struct QNode {
+  double xmin, ymin, xmax, ymax;  // bounding box
+  double sx, sy;                  // split point (box centre)
+  int child[4] = {-1, -1, -1, -1};
+  int parent = -1;
+  int depth = 0;
+  int64_t i0 = 0, i1 = 0;         // tree-order range of the node's points
+  bool leaf() const { return child[0] < 0 && child[1] < 0 && child[2] < 0 && child[3] < 0; }
+  int64_t numPoints() const { return i1 - i0; }
+};
+
+class Quadtree {
+ public:
+  // leafSize generalises LEAF_SIZE_THRESHOLD = 1 (quadtree_node.c:17): a
+  // node with more than leafSize points is split.
+  void build(double const *xy, int64_t n, int64_t leafSize);
+  Circle circle(int node) const;  // quadtree_node.c:321-330
+  std::vector<int> children(int node) const;
+  // LR level order below `node`, grouped by depth (tree_level_iter.c:12-88)
+  std::vector<std::vector<int>> levelsBelow(int node) const;
+
+  std::vector<QNode> nodes;
+  std::vector<int64_t> perm;
+  int64_t leafSize = 1;
+
+ private:
+  void split(int node, double const *px, double const *py);
+};
+
+enum BlockKind : int32_t { kFirst = 0, kMiddle = 1, kLast = 2, kDense = 3 };
+
+// One stored block of the factorization.  Geometry for the fill:
+//   first : sources = source-tree range [s0,s1); equivalent sources on `ceq`
+//           (m points), check points on `cchk` (m points)
+//   middle: sources = n points on `corig`; equivalent sources on `ceq`
+//           (m points); check points on `cchk` (m points)
+//   last  : sources = n points on `ceq`; targets = target-tree range [t0,t1)
+//   dense : sources [s0,s1), targets [t0,t1)
+struct Block {
+  int32_t kind;
+  int32_t m, n;
+  int32_t ri, ci;               // block row / column within its factor
+  int64_t s0 = 0, s1 = 0, t0 = 0, t1 = 0;
+  Circle corig, ceq, cchk;
+  int64_t arenaOff = 0;         // complex entries, column-major m x n
+};
+
+struct Factor {
+  int32_t kind;                 // 0 = block diagonal, 1 = block COO
+  int32_t nbr, nbc;
+  std::vector<int64_t> rowOff, colOff;
+  std::vector<int32_t> blocks;  // indices into Plan::blocks, stored order
+};
+
+struct Product {
+  std::vector<int32_t> factors; // stored order: [evaluation, ..., first]
+  int64_t t0, t1, s0, s1;
+};
+
+// A node of the hierarchical (HODBF) structure.
+struct PNode {
+  int32_t type;                 // 0 = block dense, 1 = product, 2 = dense
+  int32_t nr = 0, nc = 0;
+  std::vector<int64_t> rowOff, colOff;
+  std::vector<int32_t> children;
+  int32_t product = -1, block = -1;
+};
+
+struct PlanParams {
+  double k = 1;
+  int64_t leafSize = 1;
+  double rankEps = 1e-15;       // eps of the rank estimate (helm2.c:14-36)
+};
+
+struct Plan {
+  Quadtree src, tgt;
+  std::vector<Block> blocks;
+  std::vector<Factor> factors;
+  std::vector<Product> products;
+  std::vector<PNode> pnodes;
+  int32_t root = -1;
+  int64_t arenaEntries = 0;
+  // block indices in plan order (the order of the plan text); the arena
+  // stores the blocks back to back in this order
+  std::vector<int32_t> blockOrder;
+
+  std::string text() const;     // the plan grammar of the oracle driver
+};
+
+// Builds trees and the plan; throws std::runtime_error on geometry the
+// reference cannot factor.
+void makePlan(Plan &plan, PlanParams const &params, double const *srcXy,
+              int64_t nSrc, double const *tgtXy, int64_t nTgt);
+
+// ---------------------------------------------------------------------------
+// GPU descriptor tables
+// ---------------------------------------------------------------------------
+
+// One work item of an apply stage: up to kItemRows consecutive output rows of
+// one block row, accumulating over the blocks in that row.
+constexpr int kItemRows = 32;
+
+struct ApplyItem {
+  int64_t outRow;               // first output row in the workspace
+  int32_t rows;                 // <= kItemRows
+  int32_t nContrib;
+  int64_t contrib0;             // first contribution
+};
+
+struct ApplyContrib {
+  int64_t aOff;                 // arena offset of (first item row, column 0)
+  int64_t inRow;                // first input row
+  int32_t lda;                  // column stride of the block (its m)
+  int32_t n;                    // columns
+  int32_t inIsX;                // 1: input rows are in X, 0: in the workspace
+  int32_t pad;
+};
+
+struct ApplyProgram {
+  std::vector<int64_t> stageItem0;        // item range per stage (+1)
+  std::vector<ApplyItem> items;
+  std::vector<ApplyContrib> contribs;
+  int64_t wsRows = 0;                     // workspace rows
+  // final reduction: target row i sums segBase[c] + (i - segStart[s]) over
+  // contributions c of its segment s
+  std::vector<int32_t> rowSeg;            // per tree-order target row
+  std::vector<int64_t> segStart;          // first row of each segment
+  std::vector<int64_t> segContrib0;       // contribution range (+1)
+  std::vector<int64_t> segBase;           // workspace row of segment start
+  int64_t numRows = 0, numCols = 0;
+  double flopsPerRhs = 0;                 // 8 * sum m*n
+  // algorithmic traffic per stage: stored entries read, vector rows read
+  // and written (one RHS); the final sum reads sumRows and writes numRows
+  std::vector<int64_t> stageEntries, stageRowsIn, stageRowsOut;
+  int64_t sumRows = 0;
+};
+
+void makeApplyProgram(Plan const &plan, ApplyProgram &prog);
+
+// Fill descriptors for the kernel-evaluation and re-expansion kernels.
+struct FillDesc {
+  int32_t kind, m, n, pad;
+  int64_t arenaOff;
+  int64_t s0, t0;               // tree-order point offsets
+  double corig[3], ceq[3], cchk[3];
+};
+
+}  // namespace bfg

@@ -1,0 +1,212 @@
+/* bfg -- GB300-native butterfly factorization of the 2-D Helmholtz kernel.
+ *
+ * C ABI of libbfg.so.  Plain pointers and sizes only.  Every entry point
+ * returns a bfgStatus; the message of the last failure on a context is
+ * available from bfgGetErrorString.  Nothing here aborts the process and
+ * no kernel traps: failures come back as status codes.
+ *
+ * Complex numbers are interleaved (re, im) pairs: complex128 = two doubles,
+ * complex64 = two floats.  Matrices are row-major with a leading dimension
+ * in elements, as the reference's BfMatDenseComplex (rowStride = numCols,
+ * mat_dense_complex.c:2069-2087).
+ *
+ * Each declaration names the reference interface it replaces.
+ */
+#ifndef BFG_H
+#define BFG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  0..8 carry the reference's BfError numbering
+ * (error.h:3-16) so an adapter can forward them unchanged. */
+typedef enum bfgStatus {
+  BFG_OK = 0,                       /* BF_ERROR_NONE */
+  BFG_ERROR_INVALID_ARGUMENTS = 1,  /* BF_ERROR_INVALID_ARGUMENTS */
+  BFG_ERROR_RUNTIME = 2,            /* BF_ERROR_RUNTIME_ERROR */
+  BFG_ERROR_NOT_IMPLEMENTED = 3,    /* BF_ERROR_NOT_IMPLEMENTED */
+  BFG_ERROR_MEMORY = 4,             /* BF_ERROR_MEMORY_ERROR */
+  BFG_ERROR_OUT_OF_RANGE = 5,       /* BF_ERROR_OUT_OF_RANGE */
+  BFG_ERROR_INCOMPATIBLE_SHAPES = 8,/* BF_ERROR_INCOMPATIBLE_SHAPES */
+  BFG_ERROR_CUDA = 32,              /* a CUDA runtime call failed */
+  BFG_ERROR_TIMEOUT = 33,           /* a bounded device wait ran out */
+  BFG_ERROR_NUMERICAL = 34          /* e.g. an SVD that did not converge */
+} bfgStatus;
+
+/* Layer potentials, numbered as BfLayerPotential (layer_pot.h:52-65). */
+typedef enum bfgLayerPotential {
+  BFG_LAYER_POTENTIAL_SINGLE = 1,
+  BFG_LAYER_POTENTIAL_PV_DOUBLE = 2,
+  BFG_LAYER_POTENTIAL_PV_NORMAL_DERIV_SINGLE = 3,
+  BFG_LAYER_POTENTIAL_COMBINED_FIELD = 5
+} bfgLayerPotential;
+
+/* Arithmetic of an apply. */
+typedef enum bfgPrecision {
+  BFG_PRECISION_FP64 = 0,   /* complex128 factors and vectors */
+  BFG_PRECISION_FP32 = 1    /* complex64 factors and vectors, FP32 accumulate */
+} bfgPrecision;
+
+typedef struct bfgContext_s *bfgContext;
+typedef struct bfgFac_s *bfgFac;
+
+/* BfHelm2 (helm2.h:10-15) with its complex scalars split into parts. */
+typedef struct bfgHelm2 {
+  double k;
+  int32_t layerPot;           /* bfgLayerPotential */
+  int32_t reserved;
+  double alphaRe, alphaIm;    /* combined field: alpha S + beta D */
+  double betaRe, betaIm;
+} bfgHelm2;
+
+/* Knobs of the factorization.  bfgFacOptionsDefault gives the reference's
+ * behaviour exactly. */
+typedef struct bfgFacOptions {
+  int64_t leafSize;   /* split nodes with more points (reference: 1,
+                         quadtree_node.c:17) */
+  double rankEps;     /* eps in the rank estimate p = ceil(k r1 r2 / d -
+                         log10 eps) (reference: 1e-15, fac_helm2.c:102,
+                         291-296, 523; helm2.c:14-36) */
+  int32_t pinvCut;    /* 0: keep sigma >= max(m,n) eps sigma0 + eps
+                         (mat_dense_complex.c:1797-1808); 1: keep
+                         sigma >= pinvTol * sigma0 (linalg.c:26-36) */
+  int32_t reserved;
+  double pinvTol;
+} bfgFacOptions;
+
+typedef struct bfgFacStats {
+  int64_t numRows, numCols;
+  int64_t numBlocks, numFirst, numMiddle, numLast, numDense;
+  int64_t numProducts;
+  int64_t arenaEntries;       /* complex entries over all stored blocks */
+  int64_t numStages;          /* apply launches before the final sum */
+  int64_t numItems;           /* apply work items over all stages */
+  int64_t maxRank;
+  int64_t jacobiNotConverged; /* blocks whose Jacobi SVD hit the sweep cap */
+  double factorMs;            /* device time of the factorization kernels */
+  double flopsPerRhs;         /* 8 * sum over blocks of m*n */
+} bfgFacStats;
+
+/* Contexts: one CUDA device and one stream; calls on a context are
+ * serialised by the caller. */
+bfgStatus bfgContextCreate(int32_t device, bfgContext *ctx);
+bfgStatus bfgContextDestroy(bfgContext ctx);
+/* Launch on the caller's cudaStream_t (passed as void*; NULL is CUDA's
+ * legacy default stream).  A context starts on a non-blocking stream of its
+ * own; bfgContextGetStream returns the stream in use. */
+bfgStatus bfgContextSetStream(bfgContext ctx, void *cudaStream);
+bfgStatus bfgContextGetStream(bfgContext ctx, void **cudaStream);
+/* Waits for all work the context has launched. */
+bfgStatus bfgContextSynchronize(bfgContext ctx);
+char const *bfgGetErrorString(bfgContext ctx);
+
+void bfgFacOptionsDefault(bfgFacOptions *opts);
+
+/* Replaces bfQuadtreeInit for both point sets (quadtree.c:80-98) followed by
+ * bfFacHelm2MakeMultilevel (fac_helm2.h:18, fac_helm2.c:943-1002).
+ * Points are host arrays of (x, y) pairs in original order; normals may be
+ * NULL.  The factorization runs on the GPU and stays resident there. */
+bfgStatus bfgFacHelm2MakeMultilevel(bfgContext ctx, bfgHelm2 const *helm,
+                                    double const *srcXy, double const *srcNormals,
+                                    int64_t numSrc, double const *tgtXy,
+                                    double const *tgtNormals, int64_t numTgt,
+                                    bfgFacOptions const *opts, bfgFac *fac);
+/* bfMatDelete on the factorization (mat.h:57). */
+bfgStatus bfgFacDestroy(bfgFac fac);
+/* bfMatGetNumRows / bfMatGetNumCols (mat.c). */
+bfgStatus bfgFacGetShape(bfgFac fac, int64_t *numRows, int64_t *numCols);
+/* BfTree.perm of both quadtrees: tree position -> original index. */
+bfgStatus bfgFacGetPerms(bfgFac fac, int64_t *srcPerm, int64_t *tgtPerm);
+/* bfMatNumBytes (mat.h:56): bytes of the stored complex128 blocks. */
+bfgStatus bfgFacNumBytes(bfgFac fac, int64_t *numBytes);
+bfgStatus bfgFacGetStats(bfgFac fac, bfgFacStats *stats);
+/* The block structure in the grammar of the oracle's plan dump. */
+bfgStatus bfgFacDescribe(bfgFac fac, char *buf, int64_t capacity, int64_t *length);
+/* Host copy of every stored block, plan order, each column-major m x n
+ * complex128; `table` receives (kind, m, n, arena offset) per block. */
+bfgStatus bfgFacCopyBlocks(bfgFac fac, double *entries, int64_t capacityEntries,
+                           int64_t *table, int64_t capacityBlocks);
+
+/* Flags of the applies. */
+#define BFG_APPLY_ORIGINAL_ORDER 1u  /* X and Y rows in original point order */
+
+/* Y = A X -- bfMatMul (mat.c:183-185) with A the factorization.  X (numCols
+ * x numRhs) and Y (numRows x numRhs) are DEVICE pointers: complex128 for
+ * FP64, complex64 for FP32.  Rows are in tree order unless
+ * BFG_APPLY_ORIGINAL_ORDER is set.  Runs on the context's stream; returns
+ * without synchronising. */
+bfgStatus bfgFacApply(bfgFac fac, bfgPrecision precision, void const *X, int64_t ldx,
+                      int64_t numRhs, void *Y, int64_t ldy, uint32_t flags);
+
+/* The same product with HOST complex128 X and Y (the reference's contract
+ * for bfMatMul on BfMatDenseComplex operands); copies both ways and
+ * synchronises.  The precision selects the device arithmetic. */
+bfgStatus bfgFacApplyHost(bfgFac fac, bfgPrecision precision, double const *X,
+                          int64_t ldx, int64_t numRhs, double *Y, int64_t ldy,
+                          uint32_t flags);
+
+/* bfgFacApply with a CUDA event around every launch; launchMs[i] receives
+ * the device time of launch i (stages in order, then the final sum).
+ * Synchronises. */
+bfgStatus bfgFacApplyTimed(bfgFac fac, bfgPrecision precision, void const *X,
+                           int64_t ldx, int64_t numRhs, void *Y, int64_t ldy,
+                           uint32_t flags, float *launchMs, int32_t capacity,
+                           int32_t *numLaunches);
+
+/* Algorithmic work of each launch of an apply with these flags, in the
+ * order of bfgFacApplyTimed: info[3i..3i+2] = stored complex entries read,
+ * vector rows read, vector rows written (per right-hand side). */
+bfgStatus bfgFacGetLaunchInfo(bfgFac fac, uint32_t flags, int64_t *info,
+                              int32_t capacity, int32_t *numLaunches);
+
+/* Rows `rows` (tree order) of the dense FP64 product K X, evaluated on the
+ * GPU kernel by kernel -- bfHelm2GetKernelMatrix (helm2.c:282-319) times X
+ * without forming K.  X: device complex128, tree order; out: device
+ * complex128 (numRowsSel x numRhs, leading dimension ldo). */
+bfgStatus bfgFacDenseRows(bfgFac fac, int64_t const *rows, int64_t numRowsSel,
+                          void const *X, int64_t ldx, int64_t numRhs, void *out,
+                          int64_t ldo);
+
+/* bfHelm2GetKernelMatrix (helm2.c:282-319): host arrays in and out,
+ * out = row-major m x n complex128, rows = targets. */
+bfgStatus bfgHelm2KernelMatrix(bfgContext ctx, bfgHelm2 const *helm,
+                               double const *srcXy, double const *srcNormals,
+                               int64_t numSrc, double const *tgtXy,
+                               double const *tgtNormals, int64_t numTgt,
+                               double *out);
+
+/* bf_H0 / bf_H1 (bessel.c:294-308) evaluated on the GPU:
+ * out[4i..4i+3] = J0, Y0, J1, Y1 at x[i] > 0 (host arrays). */
+bfgStatus bfgBessel01(bfgContext ctx, double const *x, int64_t n, double *out);
+
+/* Host-only (no GPU needed): the quadtrees and block structure that
+ * bfgFacHelm2MakeMultilevel builds for the same inputs -- the permutations
+ * and the plan text of bfgFacDescribe.  Either output may be NULL. */
+bfgStatus bfgPlanHelm2(double k, double const *srcXy, int64_t numSrc,
+                       double const *tgtXy, int64_t numTgt,
+                       bfgFacOptions const *opts, int64_t *srcPerm,
+                       int64_t *tgtPerm, char *buf, int64_t capacity,
+                       int64_t *length);
+
+/* Host-only: the device H0/H1 evaluator's source compiled for the CPU,
+ * out[4i..4i+3] = J0, Y0, J1, Y1. */
+bfgStatus bfgBessel01Host(double const *x, int64_t n, double *out);
+
+/* The reference's seeded generator (rand.c:19-76): splitmix64 seeding
+ * xoshiro256+.  State is explicit instead of process-global. */
+typedef struct bfgRng {
+  uint64_t s[4];
+} bfgRng;
+void bfgRngSeed(bfgRng *rng, uint64_t seed);               /* bfSeed */
+double bfgRngUniform1(bfgRng *rng);                        /* bfRealUniform1 */
+void bfgRngUniform(bfgRng *rng, int64_t n, double *out);   /* bfRealUniform */
+void bfgRngComplexRandn(bfgRng *rng, int64_t n, double *out); /* bfComplexRandn, 2n doubles */
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BFG_H */

@@ -821,9 +821,67 @@ class ApplyPort:
     """The reference's apply restated in C (oracle_kernels.c), timed as the
     CPU baseline."""
 
-    def __init__(self, fac: Factorization):
-        self.terms, self.factors, self.fblocks, self.data = fac.port_arrays()
-        self.nrows = len(fac.tgt_perm)
+    def __init__(self, fac: Factorization = None):
+        self.col_major = 0
+        if fac is not None:
+            self.terms, self.factors, self.fblocks, self.data = fac.port_arrays()
+            self.nrows = len(fac.tgt_perm)
+
+    @classmethod
+    def from_plan(cls, text: str, data: np.ndarray, col_major: bool):
+        """Port over the structure of a plan text (oracle_dump grammar) with
+        the blocks stored back to back in plan order in ``data`` --
+        row-major, or column-major as in the GPU arena."""
+        root = parse_plan(text)
+        off = [0]
+
+        def take(m, n):
+            o = off[0]
+            off[0] += m * n
+            return o
+
+        terms, factors, fblocks = [], [], []
+
+        def rec(nd, r0, c0, group):
+            if isinstance(nd, BlockDense):
+                for i in range(nd.nr):
+                    for j in range(nd.nc):
+                        rec(nd.children[i * nd.nc + j], r0 + nd.row_off[i],
+                            c0 + nd.col_off[j], group if group is not None else i)
+            elif isinstance(nd, Dense):
+                b = nd.block
+                terms.append((0, group, r0, c0, b.m, b.n, 0, 0, take(b.m, b.n)))
+            else:
+                ff = len(factors)
+                offs = [[take(b.m, b.n) for b in f.blocks] for f in nd.factors]
+                for f, fo in zip(reversed(nd.factors), reversed(offs)):
+                    fb = len(fblocks)
+                    for b, o in zip(f.blocks, fo):
+                        fblocks.append((f.row_off[b.ri], f.col_off[b.ci], b.m, b.n, o))
+                    factors.append((f.row_off[-1], f.col_off[-1], fb, len(f.blocks), 0))
+                m = nd.factors[0].row_off[-1]
+                n = nd.factors[-1].col_off[-1]
+                terms.append((1, group, r0, c0, m, n, ff, len(nd.factors), 0))
+
+        rec(root, 0, 0, None)
+        if off[0] > data.size:
+            raise ValueError("block data shorter than the plan")
+        p = cls()
+        term_dt = np.dtype([("kind", "<i4"), ("group", "<i4"), ("tgtRow", "<i8"),
+                            ("srcRow", "<i8"), ("m", "<i4"), ("n", "<i4"),
+                            ("firstFactor", "<i4"), ("numFactors", "<i4"),
+                            ("dataOff", "<i8")])
+        fac_dt = np.dtype([("rows", "<i4"), ("cols", "<i4"), ("firstBlock", "<i8"),
+                           ("numBlocks", "<i4"), ("pad", "<i4")])
+        blk_dt = np.dtype([("rowOff", "<i8"), ("colOff", "<i8"), ("m", "<i4"),
+                           ("n", "<i4"), ("dataOff", "<i8")])
+        p.terms = np.array(terms, dtype=term_dt)
+        p.factors = np.array(factors, dtype=fac_dt)
+        p.fblocks = np.array(fblocks, dtype=blk_dt)
+        p.data = np.ascontiguousarray(data, dtype=np.complex128)
+        p.nrows = root.row_off[-1]
+        p.col_major = 1 if col_major else 0
+        return p
 
     def __call__(self, X: np.ndarray, nthreads: int = 1) -> np.ndarray:
         X = np.ascontiguousarray(X, dtype=np.complex128)
@@ -834,10 +892,55 @@ class ApplyPort:
         rc = lib().oracle_apply_port(
             ctypes.c_int64(len(self.terms)), _ptr(self.terms), _ptr(self.factors),
             _ptr(self.fblocks), _ptr(self.data), _ptr(X), _ptr(Y),
-            ctypes.c_int64(self.nrows), ctypes.c_int64(R), ctypes.c_int32(nthreads))
+            ctypes.c_int64(self.nrows), ctypes.c_int64(R), ctypes.c_int32(nthreads),
+            ctypes.c_int32(self.col_major))
         if rc != 0:
             raise MemoryError("apply port failed")
         return Y
+
+
+def parse_plan(text: str):
+    """Inverse of plan_text: the structure (no geometry) of a plan dump."""
+    lines = text.split("\n")
+    pos = [0]
+
+    def nxt():
+        toks = lines[pos[0]].split()
+        pos[0] += 1
+        return toks
+
+    def ints(toks):
+        return [int(t) for t in toks[1:]]
+
+    def rec():
+        t = nxt()
+        if t[0] == "BD":
+            nr, nc = int(t[1]), int(t[2])
+            ro, co = ints(nxt()), ints(nxt())
+            return BlockDense(nr, nc, ro, co, [rec() for _ in range(nr * nc)])
+        if t[0] == "PR":
+            return Product([rec() for _ in range(int(t[1]))], None, None)
+        if t[0] == "DG":
+            nb = int(t[1])
+            ro, co = ints(nxt()), ints(nxt())
+            blocks = []
+            for i in range(nb):
+                _, m, n = nxt()
+                blocks.append(Block("diag", int(m), int(n), ri=i, ci=i))
+            return Factor("DG", nb, nb, ro, co, blocks)
+        if t[0] == "CB":
+            nr, nc, nb = int(t[1]), int(t[2]), int(t[3])
+            ro, co = ints(nxt()), ints(nxt())
+            blocks = []
+            for _ in range(nb):
+                _, ri, ci, m, n = nxt()
+                blocks.append(Block("coo", int(m), int(n), ri=int(ri), ci=int(ci)))
+            return Factor("CB", nr, nc, ro, co, blocks)
+        if t[0] == "DC":
+            return Dense(Block("dense", int(t[1]), int(t[2])))
+        raise ValueError("bad plan line %r" % t)
+
+    return rec()
 
 
 def dense_rows(helm: Helm2, src_tree_pts, tgt_tree_pts, rows, X,

@@ -142,8 +142,25 @@ typedef struct {
   int64_t dataOff;
 } OracleFBlock;
 
+static int gColMajor = 0;
+
+/* Y[m x R] += A[m x n] X[n x R]; A row-major, or column-major when the
+ * blocks come straight from the GPU arena. */
 static void blockGemmAcc(cplx const *A, int32_t m, int32_t n, cplx const *X,
                          cplx *Y, int64_t R) {
+  if (gColMajor) {
+    for (int32_t j = 0; j < n; ++j) {
+      cplx const *x = X + (int64_t)j * R;
+      cplx const *a = A + (int64_t)j * m;
+      for (int32_t i = 0; i < m; ++i) {
+        cplx *y = Y + (int64_t)i * R;
+        cplx const ai = a[i];
+        for (int64_t r = 0; r < R; ++r)
+          y[r] += ai * x[r];
+      }
+    }
+    return;
+  }
   for (int32_t i = 0; i < m; ++i) {
     cplx *y = Y + (int64_t)i * R;
     for (int32_t j = 0; j < n; ++j) {
@@ -158,7 +175,8 @@ static void blockGemmAcc(cplx const *A, int32_t m, int32_t n, cplx const *X,
 int oracle_apply_port(int64_t nterm, OracleTerm const *terms,
                       OracleFactor const *factors, OracleFBlock const *fblocks,
                       cplx const *data, cplx const *X, cplx *Y, int64_t nrowsY,
-                      int64_t R, int32_t nthreads) {
+                      int64_t R, int32_t nthreads, int32_t colMajor) {
+  gColMajor = colMajor;
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #else

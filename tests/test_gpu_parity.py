@@ -1,0 +1,252 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the reference's
+own outputs (golden fixtures) and the CPU oracle on the same seeded inputs.
+
+Tolerances:
+  * integer structure (permutations, plan) -- exact;
+  * H0/H1 and kernel entries -- 1e-13 relative to glibc (the reference's
+    Bessel functions);
+  * FP64 apply -- 1e-10 relative to the reference's own A_BF X and to the
+    dense FP64 product (the reference itself reaches ~1e-12; the pseudo-
+    inverse re-expansion is ill-conditioned, so Jacobi and LAPACK SVDs give
+    factors that differ entry-wise while the operator agrees);
+  * FP32 apply -- 1e-5 relative to the FP64 apply.
+"""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, load_golden, rel_err
+from oracle import bf_oracle as O
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import butterfly_gb300 as B  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return B.default_context(0)
+
+
+_facs = {}
+
+
+def golden_fac(name, ctx):
+    if name not in _facs:
+        g = load_golden(name)
+        fac = B.FacHelm2.make_multilevel(B.Helm2(float(g["k"])), B.Quadtree(g["src"]),
+                                         B.Quadtree(g["tgt"]), context=ctx)
+        _facs[name] = (g, fac)
+    return _facs[name]
+
+
+def test_bessel_device_matches_glibc(ctx):
+    from test_host_library import glibc_h01, hankel_samples
+    x = hankel_samples(400000, seed=1)
+    b = B.bessel01(x, ctx)
+    g0, g1 = glibc_h01(x)
+    e0 = np.abs(b[:, 0] + 1j * b[:, 1] - g0) / np.abs(g0)
+    e1 = np.abs(b[:, 2] + 1j * b[:, 3] - g1) / np.abs(g1)
+    assert e0.max() < 1e-13 and e1.max() < 1e-13
+
+
+@pytest.mark.parametrize("lp", [B.LayerPot.S, B.LayerPot.D, B.LayerPot.Sp,
+                                B.LayerPot.CombinedField])
+def test_kernel_matrix_matches_oracle(ctx, lp):
+    rng = np.random.default_rng(3)
+    src = rng.uniform(-1, 1, (300, 2))
+    tgt = rng.uniform(-1, 1, (200, 2))
+    tgt[:5] = src[:5]                      # r == 0 entries must be exactly 0
+    ang = rng.uniform(0, 2 * np.pi, 300)
+    sn = np.stack([np.cos(ang), np.sin(ang)], 1)
+    ang = rng.uniform(0, 2 * np.pi, 200)
+    tn = np.stack([np.cos(ang), np.sin(ang)], 1)
+    helm = B.Helm2(37.0, lp, alpha=-37.0j, beta=1.0)
+    K = B.kernel_matrix(helm, src, tgt, sn, tn, ctx)
+    Ko = O.kernel_matrix(O.Helm2(37.0, int(lp), -37.0j, 1.0), src, tgt, sn, tn)
+    assert np.all(K[np.arange(5), np.arange(5)] == 0)
+    scale = np.abs(Ko)
+    mask = scale > 0
+    assert (np.abs(K - Ko)[mask] / scale[mask]).max() < 1e-12
+
+
+@pytest.mark.parametrize("name", list(GOLDEN_CASES))
+def test_factorization_structure_matches_reference(ctx, name):
+    g, fac = golden_fac(name, ctx)
+    assert np.array_equal(fac.src_perm, g["src_perm"].astype(np.int64))
+    assert np.array_equal(fac.tgt_perm, g["tgt_perm"].astype(np.int64))
+    assert fac.describe() == g["plan"]
+    st = fac.stats()
+    assert st["jacobiNotConverged"] == 0
+    assert fac.num_bytes() == 16 * st["arenaEntries"]
+
+
+@pytest.mark.parametrize("name", list(GOLDEN_CASES))
+def test_fp64_apply_matches_reference(ctx, name):
+    g, fac = golden_fac(name, ctx)
+    x = g["x"]
+    y = fac.apply(x)                                   # host operands, C ABI
+    assert rel_err(y, g["y_bf"]) < 1e-10
+    rows = g["dense_rows"]
+    assert rel_err(y[rows], g["y_dense"]) < 1e-10
+    # device operands give the same bits
+    xd = torch.from_numpy(x).cuda()
+    yd = fac.apply(xd).cpu().numpy()
+    assert np.array_equal(yd, y)
+
+
+def test_apply_is_deterministic_and_graph_free_of_atomics(ctx):
+    g, fac = golden_fac("c1_circle_n4096_k64", ctx)
+    xd = torch.from_numpy(g["x"]).cuda()
+    y1 = fac.apply(xd)
+    y2 = fac.apply(xd)
+    assert torch.equal(y1, y2)
+
+
+@pytest.mark.parametrize("R", [1, 2, 5, 16, 40])
+def test_multi_rhs_matches_oracle(ctx, R):
+    g, fac = golden_fac("star_n2048_k48", ctx)
+    rng = O.RefRng(100 + R)
+    X = rng.complex_randn(2048 * R).reshape(2048, R)
+    of = _oracle_fac("star_n2048_k48")
+    yo = of.apply(X)
+    y = fac.apply(X)
+    assert rel_err(y, yo) < 1e-10
+    # columns are independent: each equals the single-RHS apply
+    y0 = fac.apply(np.ascontiguousarray(X[:, :1]))
+    assert rel_err(y[:, :1], y0) < 1e-13
+
+
+_oracle = {}
+
+
+def _oracle_fac(name):
+    if name not in _oracle:
+        g = load_golden(name)
+        _oracle[name] = O.Factorization(O.Helm2(float(g["k"])), g["src"], g["tgt"])
+    return _oracle[name]
+
+
+def test_original_order_flag(ctx):
+    g, fac = golden_fac("star_n2048_k48", ctx)
+    sp, tp = fac.perms()
+    x_tree = g["x"]
+    x_orig = np.empty_like(x_tree)
+    x_orig[sp] = x_tree
+    y_tree = fac.apply(x_tree)
+    y_orig = fac.apply(x_orig, original_order=True)
+    assert rel_err(y_orig[tp], y_tree) < 1e-14
+
+
+@pytest.mark.parametrize("R", [1, 7, 64])
+def test_fp32_apply_close_to_fp64(ctx, R):
+    g, fac = golden_fac("c1_circle_n4096_k64", ctx)
+    rng = O.RefRng(5)
+    X = rng.complex_randn(4096 * R).reshape(4096, R)
+    y64 = fac.apply(torch.from_numpy(X).cuda()).cpu().numpy()
+    y32 = fac.apply(torch.from_numpy(X).cuda().to(torch.complex64), precision="fp32")
+    assert rel_err(y32.cpu().numpy().astype(np.complex128), y64) < 1e-5
+
+
+def test_blocks_solve_the_reexpansion_least_squares(ctx):
+    """Every FIRST/MIDDLE block is a least-squares re-expansion: the GPU's
+    Z_shift leaves a residual Z_equiv Z_shift - Z_orig as small as the
+    LAPACK-based oracle block does (helm2.c:321-365)."""
+    g, fac = golden_fac("star_n2048_k48", ctx)
+    of = _oracle_fac("star_n2048_k48")
+    tab, ent = fac.blocks()
+    oblocks = of.blocks()
+    assert len(oblocks) == len(tab)
+    checked = 0
+    for (kind, m, n, off), ob in zip(tab[::7], oblocks[::7]):
+        assert (m, n) == (ob.m, ob.n)
+        Z = ent[off:off + m * n].reshape(n, m).T          # column-major
+        if kind in (2, 3):                                # plain kernel blocks
+            assert rel_err(Z, ob.data) < 1e-12
+            continue
+        eq_pts, eq_nrm = O.circle_points(ob.ceq, m)
+        chk_pts, _ = O.circle_points(ob.cchk, m)
+        if ob.kind == "first":
+            s0, s1 = ob.src_range
+            orig = of.src_tree_pts[s0:s1]
+        else:
+            orig, _ = O.circle_points(ob.corig, n)
+        h = O.Helm2(of.helm.k)
+        Ze = O.kernel_matrix(h, eq_pts, chk_pts)
+        Zo = O.kernel_matrix(h, orig, chk_pts)
+        r_gpu = np.linalg.norm(Ze @ Z - Zo) / np.linalg.norm(Zo)
+        r_ora = np.linalg.norm(Ze @ ob.data - Zo) / np.linalg.norm(Zo)
+        assert r_gpu < max(1e-12, 10 * r_ora)
+        checked += 1
+    assert checked > 10
+
+
+def test_dense_rows_on_gpu_match_oracle(ctx):
+    g, fac = golden_fac("ellipse_n16384_k128", ctx)
+    xd = torch.from_numpy(g["x"]).cuda()
+    rows = g["dense_rows"][:16]
+    yd = fac.dense_rows(rows, xd, 1).cpu().numpy()
+    assert rel_err(yd, g["y_dense"][:16]) < 1e-12
+
+
+def test_tolerance_and_leaf_options_against_dense(ctx):
+    """BASELINE-style knobs (leaf size, rank tolerance, relative pseudo-
+    inverse cut) trade accuracy for size; the result is judged against the
+    dense FP64 product."""
+    src = O.uniform_square_points(4096, 0)
+    tgt = O.curve_points("circle", 4096)
+    helm = B.Helm2(64.0)
+    x_orig = O.RefRng(7).complex_randn(4096)          # indexed by original point
+    rows = np.arange(0, 4096, 64)                     # original target indices
+    yd = O.dense_rows(O.Helm2(64.0), src, tgt, rows, x_orig)[:, 0]
+    errs = {}
+    for leaf, eps in [(1, 1e-15), (64, 1e-8), (64, 1e-12)]:
+        fac = B.FacHelm2.make_multilevel(helm, B.Quadtree(src, leaf_size=leaf),
+                                         B.Quadtree(tgt, leaf_size=leaf), rank_eps=eps,
+                                         pinv_tol=eps if leaf > 1 else None, context=ctx)
+        sp, tp = fac.perms()
+        y_tree = fac.apply(x_orig[sp])
+        y_orig = np.empty_like(y_tree)
+        y_orig[tp] = y_tree
+        errs[(leaf, eps)] = rel_err(y_orig[rows], yd)
+    assert errs[(1, 1e-15)] < 1e-10
+    assert errs[(64, 1e-12)] < 1e-8
+    assert errs[(64, 1e-8)] < 1e-5
+
+
+def test_invalid_arguments_return_status(ctx):
+    with pytest.raises(B.BfgError) as e:
+        B.FacHelm2.make_multilevel(B.Helm2(-1.0), B.Quadtree(np.zeros((4, 2))), context=ctx)
+    assert e.value.status == 1
+    g, fac = golden_fac("star_n2048_k48", ctx)
+    with pytest.raises(ValueError):
+        fac.apply(np.zeros((5, 1), dtype=np.complex128))
+    with pytest.raises(B.BfgError):
+        fac.apply_device(0, 1, 1, 0, 1)
+    with pytest.raises(B.BfgError) as e:
+        B.FacHelm2.make_multilevel(B.Helm2(3.0, B.LayerPot.D), B.Quadtree(np.random.rand(64, 2)),
+                                   context=ctx)
+    assert e.value.status == 1
+
+
+def test_cfie_factorization_against_dense(ctx):
+    """Combined-field kernel (alpha S + beta D, helm2.c:228-280) with the
+    proxy map of layer_pot.h:87-93: butterfly vs dense FP64 on a circle."""
+    n = 3000
+    theta = (2 * np.pi / n) * np.arange(n)
+    pts = np.stack([np.cos(theta), np.sin(theta)], 1) * 2.0
+    nrm = np.stack([np.cos(theta), np.sin(theta)], 1)
+    tgt = O.curve_points("ellipse", n, 4.0, 3.5)
+    k = 40.0
+    helm = B.Helm2(k, B.LayerPot.CombinedField, alpha=-1j * k, beta=1.0)
+    fac = B.FacHelm2.make_multilevel(helm, B.Quadtree(pts, nrm), B.Quadtree(tgt), context=ctx)
+    rng = O.RefRng(1)
+    x = rng.complex_randn(n)
+    y = fac.apply(x)
+    sp, tp = fac.perms()
+    rows = np.arange(0, n, 50)
+    yd = O.dense_rows(O.Helm2(k, O.LP_COMBINED_FIELD, -1j * k, 1.0), pts[sp], tgt[tp], rows,
+                      x, src_normals=nrm[sp])[:, 0]
+    assert rel_err(y[rows], yd) < 1e-9
