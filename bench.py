@@ -321,24 +321,26 @@ def main():
     per = []
     for _ in range(3):
         per.append(fac.apply_timed(X.data_ptr(), R, R, Y.data_ptr(), R, head))
-    per = np.mean(np.array(per), axis=0)
+    per = np.mean(np.array(per, dtype=np.float64), axis=0)
     info = fac.launch_info()
     dom = int(np.argmax(per))
     sA = 16 if head == "fp64" else 8
     sv = 16 if head == "fp64" else 8
     alg_bytes = float(info[dom, 0] * sA + R * sv * (info[dom, 1] + info[dom, 2]))
+    launch_share = [float(v) for v in per / per.sum()]
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
         peak, peak_src = float(peaks["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         peak, peak_src = 6800.0, "fallback"
-    achieved = alg_bytes / (per[dom] / 1e3) / 1e9
+    achieved = float(alg_bytes / (per[dom] / 1e3) / 1e9)
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
             "kernel": "apply launch %d of %d" % (dom, len(per)),
-            "launch_ms": float(per[dom]),
-            "fp64_flops_per_s": float(8.0 * info[dom, 0] * R / (per[dom] / 1e3))}
+            "launch_ms": float(per[dom]), "alg_bytes": alg_bytes,
+            "launch_share": launch_share,
+            "flops_per_s": float(8.0 * info[dom, 0] * R / (per[dom] / 1e3))}
 
     # end to end through the C ABI with pinned host complex128 operands
     Xp = torch.from_numpy(Xh).pin_memory()

@@ -53,8 +53,8 @@ class _FacStatsC(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int64) for n in (
         "numRows", "numCols", "numBlocks", "numFirst", "numMiddle", "numLast",
         "numDense", "numProducts", "arenaEntries", "numStages", "numItems",
-        "maxRank", "jacobiNotConverged")] + [("factorMs", ctypes.c_double),
-                                             ("flopsPerRhs", ctypes.c_double)]
+        "maxRank", "jacobiNotConverged")] + [(n, ctypes.c_double) for n in (
+            "factorMs", "flopsPerRhs", "fillMs", "reexpSmemMs", "reexpGlobalMs")]
 
 
 class _RngC(ctypes.Structure):

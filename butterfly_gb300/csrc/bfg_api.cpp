@@ -177,6 +177,8 @@ bfg::FillDesc toDesc(bfg::Block const &b) {
 
 constexpr int64_t kSmemLimit = 220 * 1024;
 constexpr int64_t kScratchBudgetEntries = (int64_t)1 << 27;   // 2 GiB of complex128
+// ranks from which a block that misses shared memory gets a whole cluster
+constexpr int32_t kClusterMinRank = 128;
 
 void factorize(bfgFac f) {
   cudaStream_t s = f->ctx->stream;
@@ -188,7 +190,10 @@ void factorize(bfgFac f) {
 
   ck(f->arena64.ensure(std::max<int64_t>(1, plan.arenaEntries) * sizeof(double2)), "arena");
 
-  std::vector<bfg::FillDesc> fill, reSmall, reLarge, reGlobal;
+  // FIRST/MIDDLE blocks by where their Jacobi working set lives: shared
+  // memory (8 or 16 warps), global memory with one CTA, or global memory
+  // with a thread-block cluster for the largest ranks (the critical path)
+  std::vector<bfg::FillDesc> fill, reSmem8, reSmem16, reGlobal, reCluster;
   int32_t maxProxyN = 1;
   int64_t maxRank = 0;
   for (auto const &b : plan.blocks) {
@@ -197,26 +202,41 @@ void factorize(bfgFac f) {
       fill.push_back(d);
       if (b.kind == bfg::kLast) maxProxyN = std::max(maxProxyN, b.n);
       if (b.kind == bfg::kLast) maxRank = std::max<int64_t>(maxRank, b.n);
-    } else {
-      maxRank = std::max<int64_t>(maxRank, b.m);
-      int64_t smem = bfg::reexpansionSmemBytes(b.m, b.n);
-      if (smem <= kSmemLimit) {
-        if (b.m <= 16) reSmall.push_back(d);
-        else reLarge.push_back(d);
-      } else {
-        reGlobal.push_back(d);
-      }
+      continue;
     }
+    maxRank = std::max<int64_t>(maxRank, b.m);
+    if (bfg::reexpansionGeoBytes(b.m, b.n) > kSmemLimit)
+      throw BfgError{BFG_ERROR_NOT_IMPLEMENTED, "block geometry exceeds shared memory"};
+    if (b.m <= 16 && bfg::reexpansionSmemBytes(b.m, b.n, 8) <= kSmemLimit)
+      reSmem8.push_back(d);
+    else if (bfg::reexpansionSmemBytes(b.m, b.n, 16) <= kSmemLimit)
+      reSmem16.push_back(d);
+    else if (b.m >= kClusterMinRank)
+      reCluster.push_back(d);
+    else
+      reGlobal.push_back(d);
   }
   if (maxProxyN > 6000) throw BfgError{BFG_ERROR_NOT_IMPLEMENTED, "rank above 6000"};
+  // largest Jacobi first, so that the longest CTAs start in the first wave
+  auto cost = [](bfg::FillDesc const &d) {
+    return (double)d.m * d.m * (3.0 * d.m + d.n);
+  };
+  auto byCost = [&](bfg::FillDesc const &a, bfg::FillDesc const &b) { return cost(a) > cost(b); };
+  for (auto *v : {&reSmem8, &reSmem16, &reGlobal, &reCluster})
+    std::stable_sort(v->begin(), v->end(), byCost);
+  std::stable_sort(fill.begin(), fill.end(), [](bfg::FillDesc const &a, bfg::FillDesc const &b) {
+    return (int64_t)a.m * a.n > (int64_t)b.m * b.n;
+  });
 
-  DevBuf status, dFill, dSmall, dLarge, dGlobal, dScratchOff, scratch;
+  DevBuf status, dFill, dSmem8, dSmem16, dBatch, dScratchOff, dFlags, scratch;
   ck(status.ensure(sizeof(int32_t)), "status");
   ck(cudaMemsetAsync(status.p, 0, sizeof(int32_t), s), "status");
 
-  cudaEvent_t e0, e1;
+  cudaEvent_t e0, e1, eFill, eSmem;
   ck(cudaEventCreate(&e0), "event");
   ck(cudaEventCreate(&e1), "event");
+  ck(cudaEventCreate(&eFill), "event");
+  ck(cudaEventCreate(&eSmem), "event");
   ck(cudaEventRecord(e0, s), "event");
 
   bfg::KernelParams kpTrue = kernelParams(f->helm, f->helm.layerPot);
@@ -228,59 +248,73 @@ void factorize(bfgFac f) {
   ck(bfg::launchFillBlocks(dFill.as<bfg::FillDesc>(), (int32_t)fill.size(), src, tgt, kpTrue,
                            arena, maxProxyN, st, s),
      "fill kernel");
+  ck(cudaEventRecord(eFill, s), "event");
 
-  auto maxSmem = [](std::vector<bfg::FillDesc> const &v) {
+  auto maxBytes = [](std::vector<bfg::FillDesc> const &v, int warps, bool geoOnly) {
     int64_t m = 0;
-    for (auto const &d : v) m = std::max(m, bfg::reexpansionSmemBytes(d.m, d.n));
+    for (auto const &d : v)
+      m = std::max(m, geoOnly ? bfg::reexpansionGeoBytes(d.m, d.n)
+                              : bfg::reexpansionSmemBytes(d.m, d.n, warps));
     return (int32_t)m;
   };
-  upload(dSmall, reSmall, s, "descriptors");
-  ck(bfg::launchReexpansion(dSmall.as<bfg::FillDesc>(), (int32_t)reSmall.size(), src, kpProxy,
-                            f->opts.pinvCut, f->opts.pinvTol, arena, nullptr, nullptr, st, true,
-                            maxSmem(reSmall), 256, s),
+  upload(dSmem8, reSmem8, s, "descriptors");
+  ck(bfg::launchReexpansion(dSmem8.as<bfg::FillDesc>(), (int32_t)reSmem8.size(), src, kpProxy,
+                            f->opts.pinvCut, f->opts.pinvTol, arena, nullptr, nullptr, nullptr,
+                            st, 0, maxBytes(reSmem8, 8, false), 256, s),
      "re-expansion kernel");
-  upload(dLarge, reLarge, s, "descriptors");
-  ck(bfg::launchReexpansion(dLarge.as<bfg::FillDesc>(), (int32_t)reLarge.size(), src, kpProxy,
-                            f->opts.pinvCut, f->opts.pinvTol, arena, nullptr, nullptr, st, true,
-                            maxSmem(reLarge), 512, s),
+  upload(dSmem16, reSmem16, s, "descriptors");
+  ck(bfg::launchReexpansion(dSmem16.as<bfg::FillDesc>(), (int32_t)reSmem16.size(), src, kpProxy,
+                            f->opts.pinvCut, f->opts.pinvTol, arena, nullptr, nullptr, nullptr,
+                            st, 0, maxBytes(reSmem16, 16, false), 512, s),
      "re-expansion kernel");
+  ck(cudaEventRecord(eSmem, s), "event");
 
-  // blocks too large for shared memory: working matrices in global scratch,
-  // in batches bounded by the scratch budget
-  size_t i0 = 0;
-  while (i0 < reGlobal.size()) {
-    std::vector<int64_t> offs;
-    int64_t total = 0;
-    size_t i1 = i0;
-    int32_t geoBytes = 0;
-    while (i1 < reGlobal.size()) {
-      int64_t e = bfg::reexpansionScratchEntries(reGlobal[i1].m, reGlobal[i1].n);
-      if (i1 > i0 && total + e > kScratchBudgetEntries) break;
-      offs.push_back(total);
-      total += e;
-      geoBytes = std::max<int32_t>(
-          geoBytes, (int32_t)(8 * (7 * (int64_t)reGlobal[i1].m + 4 * (int64_t)reGlobal[i1].n)));
-      ++i1;
+  // global-memory working sets, in batches bounded by the scratch budget
+  int32_t const clusterCtas = bfg::reexpansionClusterCtas();
+  for (int mode = 1; mode <= 2; ++mode) {
+    std::vector<bfg::FillDesc> const &list = mode == 1 ? reGlobal : reCluster;
+    int32_t const warps = mode == 1 ? 16 : 16 * clusterCtas;
+    size_t i0 = 0;
+    while (i0 < list.size()) {
+      std::vector<int64_t> offs;
+      int64_t total = 0;
+      size_t i1 = i0;
+      while (i1 < list.size()) {
+        int64_t e = bfg::reexpansionScratchEntries(list[i1].m, warps);
+        if (i1 > i0 && total + e > kScratchBudgetEntries) break;
+        offs.push_back(total);
+        total += e;
+        ++i1;
+      }
+      std::vector<bfg::FillDesc> batch(list.begin() + (long)i0, list.begin() + (long)i1);
+      ck(scratch.ensure((size_t)total * sizeof(double2)), "re-expansion scratch");
+      ck(dFlags.ensure(batch.size() * clusterCtas * sizeof(int32_t)), "re-expansion flags");
+      upload(dBatch, batch, s, "descriptors");
+      upload(dScratchOff, offs, s, "descriptors");
+      ck(bfg::launchReexpansion(dBatch.as<bfg::FillDesc>(), (int32_t)batch.size(), src, kpProxy,
+                                f->opts.pinvCut, f->opts.pinvTol, arena, scratch.as<double2>(),
+                                dScratchOff.as<int64_t>(), dFlags.as<int32_t>(), st, mode,
+                                maxBytes(batch, 0, true), 512, s),
+         mode == 1 ? "re-expansion kernel (global)" : "re-expansion kernel (cluster)");
+      // the batch's descriptors, offsets and scratch are reused by the next
+      ck(cudaStreamSynchronize(s), "re-expansion");
+      i0 = i1;
     }
-    if (geoBytes > kSmemLimit) throw BfgError{BFG_ERROR_NOT_IMPLEMENTED, "block geometry exceeds shared memory"};
-    std::vector<bfg::FillDesc> batch(reGlobal.begin() + (long)i0, reGlobal.begin() + (long)i1);
-    ck(scratch.ensure((size_t)total * sizeof(double2)), "re-expansion scratch");
-    upload(dGlobal, batch, s, "descriptors");
-    upload(dScratchOff, offs, s, "descriptors");
-    ck(bfg::launchReexpansion(dGlobal.as<bfg::FillDesc>(), (int32_t)batch.size(), src, kpProxy,
-                              f->opts.pinvCut, f->opts.pinvTol, arena, scratch.as<double2>(),
-                              dScratchOff.as<int64_t>(), st, false, geoBytes, 512, s),
-       "re-expansion kernel (global)");
-    // the batch's descriptors and offsets must stay alive until it ran
-    ck(cudaStreamSynchronize(s), "re-expansion");
-    i0 = i1;
   }
   ck(cudaEventRecord(e1, s), "event");
   ck(cudaStreamSynchronize(s), "factorization");
-  float ms = 0;
+  float ms = 0, msFill = 0, msSmem = 0, msGlobal = 0;
   cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventElapsedTime(&msFill, e0, eFill);
+  cudaEventElapsedTime(&msSmem, eFill, eSmem);
+  cudaEventElapsedTime(&msGlobal, eSmem, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  cudaEventDestroy(eFill);
+  cudaEventDestroy(eSmem);
+  f->stats.fillMs = msFill;
+  f->stats.reexpSmemMs = msSmem;
+  f->stats.reexpGlobalMs = msGlobal;
   int32_t hst = 0;
   ck(cudaMemcpy(&hst, status.p, sizeof hst, cudaMemcpyDeviceToHost), "status");
   if (hst & bfg::kStatusBadDescriptor) throw BfgError{BFG_ERROR_RUNTIME, "bad block descriptor"};

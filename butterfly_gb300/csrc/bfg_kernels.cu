@@ -23,6 +23,8 @@
 //                          to original point order.
 #include <cuda_runtime.h>
 
+#include <cooperative_groups.h>
+
 #include <cstdint>
 
 #include "bfg_kernels.cuh"
@@ -128,29 +130,76 @@ __global__ void fillBlocksKernel(FillDesc const *__restrict__ descs, PointsDev s
 
 // ---------------------------------------------------------------------------
 // FIRST and MIDDLE blocks: proxy fills + Jacobi pseudo-inverse re-expansion
+//
+// Z_shift = pinv(Z_equiv) Z_orig with Z_equiv p x p.  One-sided Jacobi on
+// the columns of M = [Z_equiv^H ; I]: rotations Q make the top part
+// T = Z_equiv^H Q column-orthogonal (T = V S) while the bottom part
+// accumulates Q (= U).  Then pinv_k(Z_equiv) = T diag(w) Q^H with
+// w_a = 1/s_a^2 for kept singular values, 0 otherwise, and every column of
+// the output is x_j = T (w .* (Q^H z_j)), z_j = Z_orig[:, j] evaluated on
+// the fly.  Modes: 0 = M in shared memory (one CTA), 1 = M in global
+// scratch (one CTA), 2 = M in global scratch shared by a thread-block
+// cluster of kClusterCtas CTAs that split every Jacobi round and meet at
+// hardware cluster barriers.
 // ---------------------------------------------------------------------------
-template <bool kSmem>
-__global__ void reexpansionKernel(FillDesc const *__restrict__ descs, PointsDev src,
-                                  KernelParams kp, int32_t cutMode, double cutTol,
-                                  double2 *arena, double2 *scratch,
-                                  int64_t const *scratchOff, int32_t *status) {
+constexpr int kClusterCtas = 8;
+
+template <int kMode>
+struct ReexpMem {
+  static __device__ __forceinline__ double2 ld(double2 const *p) {
+    if (kMode == 2) return __ldcg(p);   // other SMs of the cluster write M
+    return *p;
+  }
+  static __device__ __forceinline__ void st(double2 *p, double2 v) {
+    if (kMode == 2) __stcg(p, v);
+    else *p = v;
+  }
+  static __device__ __forceinline__ void sync() {
+    if (kMode == 2) cooperative_groups::this_cluster().sync();
+    else __syncthreads();
+  }
+};
+
+template <int kMode>
+__global__ void __launch_bounds__(512) reexpansionKernel(
+    FillDesc const *__restrict__ descs, PointsDev src, KernelParams kp, int32_t cutMode,
+    double cutTol, double2 *arena, double2 *scratch, int64_t const *scratchOff,
+    int32_t *flags, int32_t *status) {
+  using Mem = ReexpMem<kMode>;
   extern __shared__ double2 smem2[];
-  FillDesc const d = descs[blockIdx.x];
-  int const p = d.m, n = d.n, LD = p + n;
-  double2 *M = kSmem ? smem2 : scratch + scratchOff[blockIdx.x];
-  double *geo = reinterpret_cast<double *>(kSmem ? smem2 + (int64_t)LD * p : smem2);
+  int const ctas = kMode == 2 ? kClusterCtas : 1;
+  int const blk = kMode == 2 ? (int)(blockIdx.x / kClusterCtas) : (int)blockIdx.x;
+  int const rank = kMode == 2 ? (int)(blockIdx.x % kClusterCtas) : 0;
+  FillDesc const d = descs[blk];
+  int const p = d.m, n = d.n, LD = 2 * p;
+  int const tid = threadIdx.x, nthr = blockDim.x;
+  int const lane = tid & 31, warp = tid >> 5, nWarps = nthr >> 5;
+  int const gWarp = rank * nWarps + warp, gWarps = ctas * nWarps;
+
+  // working matrix M (LD x p), then per-warp vectors (2p each), then (in a
+  // cluster) p shared squared singular values; see reexpansionScratchEntries
+  double2 *M, *wscr;
+  double *geo;
+  if (kMode == 0) {
+    M = smem2;
+    wscr = smem2 + (int64_t)LD * p;
+    geo = reinterpret_cast<double *>(wscr + (int64_t)2 * p * nWarps);
+  } else {
+    M = scratch + scratchOff[blk];
+    wscr = M + (int64_t)LD * p;
+    geo = reinterpret_cast<double *>(smem2);
+  }
+  double2 *myB = wscr + (int64_t)2 * p * (kMode == 0 ? warp : gWarp);
+  double2 *myY = myB + p;
   double *chkX = geo, *chkY = geo + p;
   double *eqX = geo + 2 * p, *eqY = geo + 3 * p, *eqNx = geo + 4 * p, *eqNy = geo + 5 * p;
   double *orX = geo + 6 * p, *orY = orX + n, *orNx = orX + 2 * n, *orNy = orX + 3 * n;
   double *wgt = orX + 4 * n;
   __shared__ int sRotated;
-
-  int const tid = threadIdx.x, nthr = blockDim.x;
-  int const lane = tid & 31, warp = tid >> 5, nWarps = nthr >> 5;
   bool const useSrcN = kp.layerPot == kLpPvDouble || kp.layerPot == kLpCombinedField;
 
-  // proxy geometry: check points on cchk and equivalent sources on ceq share
-  // theta_a = (2 pi / p) a (circle.c:12-58)
+  // proxy geometry (every CTA of a cluster keeps its own copy); check points
+  // on cchk and equivalent sources on ceq share theta_a = (2 pi / p) a
   {
     double const scale = kTwoPiD / (double)p;
     for (int a = tid; a < p; a += nthr) {
@@ -185,22 +234,22 @@ __global__ void reexpansionKernel(FillDesc const *__restrict__ descs, PointsDev 
   }
   __syncthreads();
 
-  // M[a*LD + r] = conj(K(chk_a, src_r)), src_r = eq_r (r < p) or orig_{r-p}
+  // M[a*LD + r] = conj(K(chk_a, eq_r)) for r < p, identity below
   {
     int64_t const total = (int64_t)LD * p;
-    for (int64_t e = tid; e < total; e += nthr) {
+    for (int64_t e = (int64_t)rank * nthr + tid; e < total; e += (int64_t)ctas * nthr) {
       int const a = (int)(e / LD), r = (int)(e % LD);
-      double sx, sy, snx, sny;
+      double2 v;
       if (r < p) {
-        sx = eqX[r]; sy = eqY[r]; snx = eqNx[r]; sny = eqNy[r];
+        double2 k = kernelValue(kp, chkX[a], chkY[a], 0.0, 0.0, eqX[r], eqY[r], eqNx[r], eqNy[r]);
+        v = make_double2(k.x, -k.y);
       } else {
-        sx = orX[r - p]; sy = orY[r - p]; snx = orNx[r - p]; sny = orNy[r - p];
+        v = make_double2(r - p == a ? 1.0 : 0.0, 0.0);
       }
-      double2 v = kernelValue(kp, chkX[a], chkY[a], 0.0, 0.0, sx, sy, snx, sny);
-      M[e] = make_double2(v.x, -v.y);
+      Mem::st(M + e, v);
     }
   }
-  __syncthreads();
+  Mem::sync();
 
   // one-sided Jacobi, round-robin pair schedule
   int const P = p + (p & 1);
@@ -211,7 +260,7 @@ __global__ void reexpansionKernel(FillDesc const *__restrict__ descs, PointsDev 
     if (tid == 0) sRotated = 0;
     __syncthreads();
     for (int round = 0; round < P - 1; ++round) {
-      for (int pr = warp; pr < nPairs; pr += nWarps) {
+      for (int pr = gWarp; pr < nPairs; pr += gWarps) {
         int i, j;
         if (pr == 0) {
           i = round;
@@ -224,7 +273,7 @@ __global__ void reexpansionKernel(FillDesc const *__restrict__ descs, PointsDev 
         double2 *ci = M + (int64_t)i * LD, *cj = M + (int64_t)j * LD;
         double al = 0, be = 0, gr = 0, gi = 0;
         for (int r = lane; r < p; r += 32) {
-          double2 x = ci[r], y = cj[r];
+          double2 x = Mem::ld(ci + r), y = Mem::ld(cj + r);
           al += x.x * x.x + x.y * x.y;
           be += y.x * y.x + y.y * y.y;
           gr += x.x * y.x + x.y * y.y;     // conj(x) y
@@ -241,33 +290,52 @@ __global__ void reexpansionKernel(FillDesc const *__restrict__ descs, PointsDev 
           double const c = 1.0 / sqrt(1.0 + t * t), s = c * t;
           double const er = gr / ag, ei = -gi / ag;   // exp(-i phi) = conj(gamma)/|gamma|
           for (int r = lane; r < LD; r += 32) {
-            double2 x = ci[r], y = cj[r];
+            double2 x = Mem::ld(ci + r), y = Mem::ld(cj + r);
             double const ytr = y.x * er - y.y * ei, yti = y.x * ei + y.y * er;
-            ci[r] = make_double2(c * x.x - s * ytr, c * x.y - s * yti);
-            cj[r] = make_double2(s * x.x + c * ytr, s * x.y + c * yti);
+            Mem::st(ci + r, make_double2(c * x.x - s * ytr, c * x.y - s * yti));
+            Mem::st(cj + r, make_double2(s * x.x + c * ytr, s * x.y + c * yti));
           }
           if (lane == 0) sRotated = 1;
         }
       }
-      __syncthreads();
+      Mem::sync();
     }
-    int const rotated = sRotated;
+    int rotated = sRotated;
+    if (kMode == 2) {
+      // cluster-wide OR of the CTAs' flags, read after a barrier so every CTA
+      // takes the same exit decision
+      if (tid == 0) __stcg(flags + (int64_t)blk * kClusterCtas + rank, rotated);
+      Mem::sync();
+      rotated = 0;
+      for (int q = 0; q < kClusterCtas; ++q)
+        rotated |= __ldcg(flags + (int64_t)blk * kClusterCtas + q);
+    }
     __syncthreads();
     if (!rotated) {
       converged = true;
       break;
     }
   }
-  if (!converged && tid == 0) atomicOr(status, kStatusJacobiNotConverged);
+  if (!converged && tid == 0 && rank == 0) atomicOr(status, kStatusJacobiNotConverged);
 
   // singular values and the pseudo-inverse cut (mat_dense_complex.c:1797-1808)
-  for (int a = warp; a < p; a += nWarps) {
+  double2 *wg = kMode == 2 ? wscr + (int64_t)2 * p * gWarps : nullptr;   // shared sigma^2
+  for (int a = gWarp; a < p; a += gWarps) {
     double2 const *ca = M + (int64_t)a * LD;
     double s2 = 0;
-    for (int r = lane; r < p; r += 32) s2 += ca[r].x * ca[r].x + ca[r].y * ca[r].y;
+    for (int r = lane; r < p; r += 32) {
+      double2 v = Mem::ld(ca + r);
+      s2 += v.x * v.x + v.y * v.y;
+    }
     s2 = warpSum(s2);
-    if (lane == 0) wgt[a] = s2;
+    if (lane == 0) {
+      if (kMode == 2) Mem::st(wg + a, make_double2(s2, 0.0));
+      else wgt[a] = s2;
+    }
   }
+  Mem::sync();
+  if (kMode == 2)
+    for (int a = tid; a < p; a += nthr) wgt[a] = Mem::ld(wg + a).x;
   __syncthreads();
   if (tid == 0) {
     double smax = 0;
@@ -280,20 +348,44 @@ __global__ void reexpansionKernel(FillDesc const *__restrict__ descs, PointsDev 
   }
   __syncthreads();
 
-  // Z_shift[i, j] = sum_a top[i,a] conj(bottom[j,a]) / s_a^2, column-major
+  // x_j = T (w .* (Q^H z_j)); one warp per output column
   double2 *out = arena + d.arenaOff;
-  int64_t const total = (int64_t)p * n;
-  for (int64_t e = tid; e < total; e += nthr) {
-    int const i = (int)(e % p), j = (int)(e / p);
-    double sr = 0, si = 0;
+  for (int j = gWarp; j < n; j += gWarps) {
+    for (int r = lane; r < p; r += 32) {
+      double2 z = kernelValue(kp, chkX[r], chkY[r], 0.0, 0.0, orX[j], orY[j], orNx[j], orNy[j]);
+      myB[r] = z;
+    }
+    __syncwarp();
     for (int a = 0; a < p; ++a) {
       double const w = wgt[a];
-      if (w == 0.0) continue;
-      double2 const t = M[(int64_t)a * LD + i], b = M[(int64_t)a * LD + p + j];
-      sr += w * (t.x * b.x + t.y * b.y);   // t * conj(b)
-      si += w * (t.y * b.x - t.x * b.y);
+      if (w == 0.0) {
+        if (lane == 0) myY[a] = make_double2(0.0, 0.0);
+        continue;
+      }
+      double2 const *qa = M + (int64_t)a * LD + p;
+      double yr = 0, yi = 0;
+      for (int r = lane; r < p; r += 32) {
+        double2 q = Mem::ld(qa + r), z = myB[r];
+        yr += q.x * z.x + q.y * z.y;        // conj(q) z
+        yi += q.x * z.y - q.y * z.x;
+      }
+      yr = warpSum(yr);
+      yi = warpSum(yi);
+      if (lane == 0) myY[a] = make_double2(w * yr, w * yi);
     }
-    out[e] = make_double2(sr, si);
+    __syncwarp();
+    for (int i = lane; i < p; i += 32) {
+      double sr = 0, si = 0;
+      for (int a = 0; a < p; ++a) {
+        double2 const y = myY[a];
+        if (y.x == 0.0 && y.y == 0.0) continue;
+        double2 const t = Mem::ld(M + (int64_t)a * LD + i);
+        sr += t.x * y.x - t.y * y.y;
+        si += t.x * y.y + t.y * y.x;
+      }
+      out[(int64_t)j * p + i] = make_double2(sr, si);
+    }
+    __syncwarp();
   }
 }
 
@@ -413,17 +505,21 @@ __device__ __forceinline__ T2 mk2(typename Real<T2>::T a, typename Real<T2>::T b
   return v;
 }
 
-// R == 1: one warp per item, lane = output row
+// R == 1: one CTA of 8 warps per item; lane = output row, warp w takes the
+// columns j = w, w + 8, ... of every block in the row, four columns in
+// flight at once; the 8 partial sums are reduced in shared memory in a
+// fixed order.
+constexpr int kGemvWarps = 8;
+
 template <typename T2>
-__global__ void applyGemvKernel(ApplyItem const *__restrict__ items, int64_t nItems,
-                                ApplyContrib const *__restrict__ contribs,
-                                T2 const *__restrict__ arena, T2 const *__restrict__ X,
-                                int64_t ldx, T2 *__restrict__ W) {
+__global__ void __launch_bounds__(32 * kGemvWarps)
+applyGemvKernel(ApplyItem const *__restrict__ items, ApplyContrib const *__restrict__ contribs,
+                T2 const *__restrict__ arena, T2 const *__restrict__ X, int64_t ldx,
+                T2 *__restrict__ W) {
   using T = typename Real<T2>::T;
-  int64_t const item = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (item >= nItems) return;
-  int const lane = threadIdx.x & 31;
-  ApplyItem const it = items[item];
+  __shared__ T2 part[kGemvWarps][32];
+  int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  ApplyItem const it = items[blockIdx.x];
   bool const active = lane < it.rows;
   T accr = 0, acci = 0;
   for (int c = 0; c < it.nContrib; ++c) {
@@ -433,19 +529,20 @@ __global__ void applyGemvKernel(ApplyItem const *__restrict__ items, int64_t nIt
     int64_t const xs = cb.inIsX ? ldx : 1;
     int const n = cb.n;
     int64_t const lda = cb.lda;
-    int j = 0;
-    for (; j + 4 <= n; j += 4) {
+    int j = warp;
+    constexpr int S = kGemvWarps;
+    for (; j + 3 * S < n; j += 4 * S) {
       T2 a0, a1, a2, a3;
       if (active) {
-        a0 = a[(j + 0) * lda];
-        a1 = a[(j + 1) * lda];
-        a2 = a[(j + 2) * lda];
-        a3 = a[(j + 3) * lda];
+        a0 = a[(int64_t)(j + 0 * S) * lda];
+        a1 = a[(int64_t)(j + 1 * S) * lda];
+        a2 = a[(int64_t)(j + 2 * S) * lda];
+        a3 = a[(int64_t)(j + 3 * S) * lda];
       } else {
         a0 = a1 = a2 = a3 = mk2<T2>(0, 0);
       }
-      T2 const x0 = x[(j + 0) * xs], x1 = x[(j + 1) * xs];
-      T2 const x2 = x[(j + 2) * xs], x3 = x[(j + 3) * xs];
+      T2 const x0 = x[(j + 0 * S) * xs], x1 = x[(j + 1 * S) * xs];
+      T2 const x2 = x[(j + 2 * S) * xs], x3 = x[(j + 3 * S) * xs];
       accr += a0.x * x0.x - a0.y * x0.y;
       acci += a0.x * x0.y + a0.y * x0.x;
       accr += a1.x * x1.x - a1.y * x1.y;
@@ -455,14 +552,24 @@ __global__ void applyGemvKernel(ApplyItem const *__restrict__ items, int64_t nIt
       accr += a3.x * x3.x - a3.y * x3.y;
       acci += a3.x * x3.y + a3.y * x3.x;
     }
-    for (; j < n; ++j) {
-      T2 const a0 = active ? a[j * lda] : mk2<T2>(0, 0);
+    for (; j < n; j += S) {
+      T2 const a0 = active ? a[(int64_t)j * lda] : mk2<T2>(0, 0);
       T2 const x0 = x[j * xs];
       accr += a0.x * x0.x - a0.y * x0.y;
       acci += a0.x * x0.y + a0.y * x0.x;
     }
   }
-  if (active) W[it.outRow + lane] = mk2<T2>(accr, acci);
+  part[warp][lane] = mk2<T2>(accr, acci);
+  __syncthreads();
+  if (warp == 0 && active) {
+    T sr = 0, si = 0;
+#pragma unroll
+    for (int w = 0; w < kGemvWarps; ++w) {
+      sr += part[w][lane].x;
+      si += part[w][lane].y;
+    }
+    W[it.outRow + lane] = mk2<T2>(sr, si);
+  }
 }
 
 // R > 1: one CTA per (item, RHS tile of RT columns); 32 rows x RT outputs,
@@ -572,14 +679,22 @@ int gridFor(int64_t total, int threads) {
 
 }  // namespace
 
-int64_t reexpansionSmemBytes(int32_t m, int32_t n) {
-  return (int64_t)16 * (m + n) * m + (int64_t)8 * (7 * (int64_t)m + 4 * (int64_t)n);
+int64_t reexpansionSmemBytes(int32_t m, int32_t n, int32_t warps) {
+  return (int64_t)16 * (2 * (int64_t)m * m + 2 * (int64_t)m * warps) +
+         reexpansionGeoBytes(m, n);
 }
 
-int64_t reexpansionScratchEntries(int32_t m, int32_t n) {
-  int64_t e = (int64_t)(m + n) * m;
+int64_t reexpansionGeoBytes(int32_t m, int32_t n) {
+  return (int64_t)8 * (7 * (int64_t)m + 4 * (int64_t)n);
+}
+
+int64_t reexpansionScratchEntries(int32_t m, int32_t warps) {
+  // M (2m x m), 2m per warp, m shared squared singular values
+  int64_t e = 2 * (int64_t)m * m + 2 * (int64_t)m * warps + m;
   return (e + 15) & ~int64_t(15);
 }
+
+int32_t reexpansionClusterCtas() { return kClusterCtas; }
 
 cudaError_t launchFillBlocks(FillDesc const *descs, int32_t nDesc, PointsDev src,
                              PointsDev tgt, KernelParams kp, double2 *arena,
@@ -595,23 +710,42 @@ cudaError_t launchFillBlocks(FillDesc const *descs, int32_t nDesc, PointsDev src
 
 cudaError_t launchReexpansion(FillDesc const *descs, int32_t nDesc, PointsDev src,
                               KernelParams kp, int32_t cutMode, double cutTol,
-                              double2 *arena, double2 *scratch,
-                              int64_t const *scratchOff, int32_t *status, bool smem,
-                              int32_t maxSmemBytes, int32_t threads, cudaStream_t stream) {
+                              double2 *arena, double2 *scratch, int64_t const *scratchOff,
+                              int32_t *flags, int32_t *status, int32_t mode,
+                              int32_t smemBytes, int32_t threads, cudaStream_t stream) {
   if (nDesc == 0) return cudaSuccess;
   cudaError_t e;
-  if (smem) {
-    e = cudaFuncSetAttribute(reexpansionKernel<true>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmemBytes);
+  if (mode == 0) {
+    e = cudaFuncSetAttribute(reexpansionKernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smemBytes);
     if (e != cudaSuccess) return e;
-    reexpansionKernel<true><<<nDesc, threads, maxSmemBytes, stream>>>(
-        descs, src, kp, cutMode, cutTol, arena, scratch, scratchOff, status);
+    reexpansionKernel<0><<<nDesc, threads, smemBytes, stream>>>(
+        descs, src, kp, cutMode, cutTol, arena, scratch, scratchOff, flags, status);
+  } else if (mode == 1) {
+    e = cudaFuncSetAttribute(reexpansionKernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smemBytes);
+    if (e != cudaSuccess) return e;
+    reexpansionKernel<1><<<nDesc, threads, smemBytes, stream>>>(
+        descs, src, kp, cutMode, cutTol, arena, scratch, scratchOff, flags, status);
   } else {
-    e = cudaFuncSetAttribute(reexpansionKernel<false>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, maxSmemBytes);
+    e = cudaFuncSetAttribute(reexpansionKernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smemBytes);
     if (e != cudaSuccess) return e;
-    reexpansionKernel<false><<<nDesc, threads, maxSmemBytes, stream>>>(
-        descs, src, kp, cutMode, cutTol, arena, scratch, scratchOff, status);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)nDesc * kClusterCtas, 1, 1);
+    cfg.blockDim = dim3((unsigned)threads, 1, 1);
+    cfg.dynamicSmemBytes = (size_t)smemBytes;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kClusterCtas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, reexpansionKernel<2>, descs, src, kp, cutMode, cutTol, arena,
+                           scratch, scratchOff, flags, status);
+    if (e != cudaSuccess) return e;
   }
   return cudaGetLastError();
 }
@@ -666,10 +800,8 @@ cudaError_t launchApplyStage(ApplyItem const *items, int64_t nItems,
                              cudaStream_t stream) {
   if (nItems == 0) return cudaSuccess;
   if (R == 1) {
-    int const warps = 8;
-    unsigned const grid = (unsigned)((nItems + warps - 1) / warps);
-    applyGemvKernel<T2><<<grid, 32 * warps, 0, stream>>>(items, nItems, contribs, arena, X,
-                                                         ldx, W);
+    applyGemvKernel<T2><<<(unsigned)nItems, 32 * kGemvWarps, 0, stream>>>(items, contribs,
+                                                                          arena, X, ldx, W);
   } else if (R <= 8) {
     dim3 grid((unsigned)nItems, 1);
     applyTileKernel<T2, 8><<<grid, 256, 0, stream>>>(items, contribs, arena, X, ldx, W, R);

@@ -43,19 +43,23 @@ cudaError_t launchFillBlocks(FillDesc const *descs, int32_t nDesc, PointsDev src
                              int32_t maxProxyN, int32_t *status, cudaStream_t stream);
 
 // Fills FIRST/MIDDLE blocks: proxy kernel matrices + pseudo-inverse
-// re-expansion.  `smem` selects the shared-memory variant (every block
-// must fit); otherwise `scratch` holds each CTA's working matrix at
-// scratchOff[cta] (complex entries).
+// re-expansion.  mode 0: working matrix in shared memory (smemBytes =
+// reexpansionSmemBytes); mode 1: in global `scratch` at scratchOff[block],
+// one CTA per block; mode 2: in global scratch, one thread-block cluster of
+// reexpansionClusterCtas() CTAs per block, `flags` holding one int per CTA.
+// Modes 1 and 2 take smemBytes = reexpansionGeoBytes of the largest block.
 cudaError_t launchReexpansion(FillDesc const *descs, int32_t nDesc, PointsDev src,
                               KernelParams kp, int32_t cutMode, double cutTol,
-                              double2 *arena, double2 *scratch,
-                              int64_t const *scratchOff, int32_t *status,
-                              bool smem, int32_t maxSmemBytes, int32_t threads,
-                              cudaStream_t stream);
+                              double2 *arena, double2 *scratch, int64_t const *scratchOff,
+                              int32_t *flags, int32_t *status, int32_t mode,
+                              int32_t smemBytes, int32_t threads, cudaStream_t stream);
 
-// Shared-memory bytes the re-expansion of an m x n block needs.
-int64_t reexpansionSmemBytes(int32_t m, int32_t n);
-int64_t reexpansionScratchEntries(int32_t m, int32_t n);
+int64_t reexpansionSmemBytes(int32_t m, int32_t n, int32_t warps);
+int64_t reexpansionGeoBytes(int32_t m, int32_t n);
+// complex entries of global scratch one block needs; `warps` = all warps
+// working on it (threads/32 times the CTAs per block)
+int64_t reexpansionScratchEntries(int32_t m, int32_t warps);
+int32_t reexpansionClusterCtas();
 
 // Dense kernel rows: out[s*ldo + r] = sum_j K(t_rows[s], src_j) x[j*ldx + r]
 cudaError_t launchDenseRows(PointsDev src, int64_t nSrc, PointsDev tgt,

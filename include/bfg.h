@@ -88,6 +88,9 @@ typedef struct bfgFacStats {
   int64_t jacobiNotConverged; /* blocks whose Jacobi SVD hit the sweep cap */
   double factorMs;            /* device time of the factorization kernels */
   double flopsPerRhs;         /* 8 * sum over blocks of m*n */
+  double fillMs;              /* evaluation and dense blocks */
+  double reexpSmemMs;         /* re-expansions held in shared memory */
+  double reexpGlobalMs;       /* re-expansions held in global memory */
 } bfgFacStats;
 
 /* Contexts: one CUDA device and one stream; calls on a context are
