@@ -509,3 +509,171 @@ def curve_points(kind: str, n: int, a: float = 3.0, b: float = 2.0, amp: float =
         r = a + amp * np.cos(lobes * theta)
         return np.stack([r * np.cos(theta), r * np.sin(theta)], axis=1)
     raise ValueError(kind)
+
+
+# ---------------------------------------------------------------------------
+# boundary-integral systems and GMRES
+# ---------------------------------------------------------------------------
+class _GmresResultC(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int64), ("relResidual", ctypes.c_double),
+                ("trueRelResidual", ctypes.c_double), ("seconds", ctypes.c_double),
+                ("converged", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+PRECOND = {"none": 0, "block_jacobi": 1, "user": 2}
+_PRECOND_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                               ctypes.c_void_p)
+
+
+def _solver_sigs():
+    L = lib()
+    if getattr(L, "_solver_sigs", False):
+        return L
+    sig = {
+        "bfgSystemCreate": [_VP, _VP, ctypes.POINTER(_Helm2C), _VP, _VP, _VP, _VP, _I64,
+                            ctypes.c_int32, ctypes.c_double, ctypes.POINTER(_VP)],
+        "bfgSystemDestroy": [_VP],
+        "bfgSystemApply": [_VP, _VP, _VP],
+        "bfgSystemBuildBlockJacobi": [_VP],
+        "bfgSystemApplyBlockJacobi": [_VP, _VP, _VP],
+        "bfgSolveGmres": [_VP, _VP, _VP, ctypes.c_double, _I64, ctypes.c_int32, _PRECOND_FN,
+                          _VP, ctypes.POINTER(_GmresResultC)],
+    }
+    for name, args in sig.items():
+        getattr(L, name).argtypes = args
+        getattr(L, name).restype = ctypes.c_int
+    L.bfgSystemGetErrorString.argtypes = [_VP]
+    L.bfgSystemGetErrorString.restype = ctypes.c_char_p
+    L._solver_sigs = True
+    return L
+
+
+class System:
+    """A = diag_shift I + (K + C) diag(w) on a factorization K (original point
+    order): the operator of the reference's assembleButterfliedK
+    (multiple_scattering_context.c:457-507)."""
+
+    def __init__(self, fac: "Fac", points, normals, weights, curve_offsets,
+                 kr_order: int = 6, diag_shift: float = 0.5):
+        L = _solver_sigs()
+        self.fac, self.ctx = fac, fac.ctx
+        pts, nrm = _xy(points), _xy(normals)
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        off = np.ascontiguousarray(curve_offsets, dtype=np.int64)
+        h = _VP()
+        hc = fac.helm._c()
+        st = L.bfgSystemCreate(self.ctx.handle, fac.handle, ctypes.byref(hc), _ptr(pts), _ptr(nrm),
+                               _ptr(w), _ptr(off), len(off) - 1, int(kr_order), float(diag_shift),
+                               ctypes.byref(h))
+        if st != BFG_OK:
+            raise BfgError(st, "bfgSystemCreate failed")
+        self.handle = h
+        self.n = len(pts)
+        _live_facs.add(self)
+
+    def _check(self, st, what):
+        if st != BFG_OK:
+            msg = _solver_sigs().bfgSystemGetErrorString(self.handle).decode()
+            raise BfgError(st, "%s: %s" % (what, msg))
+
+    def close(self):
+        if getattr(self, "handle", None) and _lib is not None:
+            _lib.bfgSystemDestroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        self.close()
+
+    def _stream(self, t):
+        import torch
+        return self.ctx.on_stream(torch.cuda.current_stream(t.device).cuda_stream)
+
+    def apply(self, x):
+        import torch
+        x = x.to(torch.complex128).contiguous()
+        y = torch.empty_like(x)
+        with self._stream(x):
+            self._check(_solver_sigs().bfgSystemApply(self.handle, _VP(x.data_ptr()),
+                                                      _VP(y.data_ptr())), "apply")
+        return y
+
+    def build_block_jacobi(self):
+        import torch
+        with self.ctx.on_stream(torch.cuda.current_stream().cuda_stream):
+            self._check(_solver_sigs().bfgSystemBuildBlockJacobi(self.handle), "block-Jacobi")
+
+    def apply_block_jacobi(self, r):
+        import torch
+        r = r.to(torch.complex128).contiguous()
+        z = torch.empty_like(r)
+        with self._stream(r):
+            self._check(_solver_sigs().bfgSystemApplyBlockJacobi(self.handle, _VP(r.data_ptr()),
+                                                                 _VP(z.data_ptr())), "precond")
+        return z
+
+
+def solve_gmres(system: System, b, x0=None, tol: float = 1e-8, max_num_iter: int = None,
+                precond="block_jacobi"):
+    """Right-preconditioned flexible GMRES on the GPU (bfSolveGMRES,
+    linalg.c:47-317, with the preconditioner on the right).  ``precond``:
+    "none", "block_jacobi", or a callable (r_ptr, z_ptr, stream_ptr) -> None
+    applying z = M r to device complex128 vectors.  Returns (x, info)."""
+    import torch
+    L = _solver_sigs()
+    b = b.to(torch.complex128).contiguous()
+    x = torch.zeros_like(b) if x0 is None else x0.to(torch.complex128).contiguous().clone()
+    m = system.n if max_num_iter is None else int(max_num_iter)
+    fn = _PRECOND_FN()
+    mode = PRECOND["user"] if callable(precond) else PRECOND[precond]
+    if callable(precond):
+        def _cb(user, r, z, stream):
+            try:
+                precond(r, z, stream)
+                return 0
+            except Exception:           # reported as a runtime error
+                return 2
+        fn = _PRECOND_FN(_cb)
+    res = _GmresResultC()
+    with system.ctx.on_stream(torch.cuda.current_stream(b.device).cuda_stream):
+        st = L.bfgSolveGmres(system.handle, _VP(b.data_ptr()), _VP(x.data_ptr()), float(tol), m,
+                             mode, fn, None, ctypes.byref(res))
+    system._check(st, "gmres")
+    info = {name: getattr(res, name) for name, _ in res._fields_ if name != "reserved"}
+    return x, info
+
+
+def scattering_geometry(num: int = 64, k: float = 200.0, ppw: float = 12.0,
+                        rmin: float = 0.05, rmax: float = 0.15, box: float = 2.0,
+                        gap: float = 0.05, seed: int = 0, max_tries: int = 1000000):
+    """Circular scatterers placed by seeded rejection sampling in
+    [-box, box]^2 with gaps >= gap, radii uniform in [rmin, rmax]; each
+    discretised like bfEllipseSampleLinspaced (ellipse.c) with
+    n = floor(perimeter / h) + 1 points (multiple_scattering_context.c:
+    351-353), h = 2 pi / (ppw k).  Returns (points, normals, weights,
+    offsets, circles)."""
+    rng = Rng(seed)
+    circles = []
+    tries = 0
+    while len(circles) < num:
+        tries += 1
+        if tries > max_tries:
+            raise RuntimeError("could not place %d scatterers" % num)
+        r = rmin + (rmax - rmin) * rng.uniform(1)[0]
+        u = rng.uniform(2)
+        cx = -box + r + (2 * (box - r)) * u[0]
+        cy = -box + r + (2 * (box - r)) * u[1]
+        if all(np.hypot(cx - c[0], cy - c[1]) >= r + c[2] + gap for c in circles):
+            circles.append((cx, cy, r))
+    h = 2 * np.pi / (ppw * k)
+    pts, nrm, wts, off = [], [], [], [0]
+    for cx, cy, r in circles:
+        n = int(np.floor(2 * np.pi * r / h)) + 1
+        dt = 6.283185307179586 / n
+        th = dt * np.arange(n)
+        c, s = np.cos(th), np.sin(th)
+        pts.append(np.stack([cx + r * c, cy + r * s], 1))
+        nrm.append(np.stack([c, s], 1))
+        wts.append(np.full(n, dt * r))
+        off.append(off[-1] + n)
+    return (np.concatenate(pts), np.concatenate(nrm), np.concatenate(wts),
+            np.array(off, dtype=np.int64), np.array(circles))

@@ -7,12 +7,7 @@
 //  * reexpansionKernel     FIRST/MIDDLE blocks: both proxy kernel matrices
 //                          (helm2.c:321-365) plus the pseudo-inverse
 //                          least-squares solve (mat_dense_complex.c:1768-1849)
-//                          in one CTA.  The SVD is a one-sided (Hestenes)
-//                          Jacobi on the stacked matrix M = [Z_equiv^H ;
-//                          Z_orig^H]: rotating columns until the top part is
-//                          orthogonal gives top = V S and bottom = Z_orig^H U,
-//                          so Z_shift = sum_a top_a conj(bottom_a)^T / s_a^2
-//                          over kept singular values, with no U or V stored.
+//                          by a one-sided Jacobi SVD (details at the kernel).
 //  * applyGemvKernel /     one stage of the staged apply (single / many RHS),
 //    applyTileKernel       each item a row chunk of one block row summing its
 //                          blocks in order; no atomics, so results are
@@ -26,6 +21,8 @@
 #include <cooperative_groups.h>
 
 #include <cstdint>
+#include <cstdlib>
+#include <cstring>
 
 #include "bfg_kernels.cuh"
 #include "hankel.cuh"
@@ -574,6 +571,70 @@ applyGemvKernel(ApplyItem const *__restrict__ items, ApplyContrib const *__restr
 
 // R > 1: one CTA per (item, RHS tile of RT columns); 32 rows x RT outputs,
 // K staged through shared memory in chunks of KC columns.
+// R > 1, register-blocked: one warp per (item, RHS tile of 4*RPT columns);
+// lane -> 4 consecutive rows x RPT consecutive RHS (8 row groups x 4 RHS
+// groups), operands read straight from global memory (the 8 lanes that share
+// a row group, and the 8 that share an RHS group, hit the same L1 lines).
+// Each column k costs 4 + RPT loads for 4*RPT complex MACs per lane.
+constexpr int kMicroWarps = 4;
+
+template <typename T2, int RPT>
+__global__ void __launch_bounds__(32 * kMicroWarps) applyMicroKernel(
+    ApplyItem const *__restrict__ items, int64_t nItems,
+    ApplyContrib const *__restrict__ contribs, T2 const *__restrict__ arena,
+    T2 const *__restrict__ X, int64_t ldx, T2 *__restrict__ W, int64_t R) {
+  using T = typename Real<T2>::T;
+  int64_t const item = (int64_t)blockIdx.x * kMicroWarps + (threadIdx.x >> 5);
+  if (item >= nItems) return;
+  int const lane = threadIdx.x & 31;
+  int const rg = lane & 7, cg = lane >> 3;
+  ApplyItem const it = items[item];
+  int const r0 = rg * 4;
+  int64_t const c0 = (int64_t)blockIdx.y * (4 * RPT) + cg * RPT;
+  bool rowOk[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) rowOk[q] = r0 + q < it.rows;
+  bool colOk[RPT];
+#pragma unroll
+  for (int q = 0; q < RPT; ++q) colOk[q] = c0 + q < R;
+  T accr[4][RPT], acci[4][RPT];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) accr[i][q] = acci[i][q] = 0;
+  for (int cbi = 0; cbi < it.nContrib; ++cbi) {
+    ApplyContrib const cb = contribs[it.contrib0 + cbi];
+    T2 const *a = arena + cb.aOff + r0;
+    T2 const *xin = (cb.inIsX ? X + cb.inRow * ldx : W + cb.inRow * R) + c0;
+    int64_t const xld = cb.inIsX ? ldx : R;
+    int64_t const lda = cb.lda;
+#pragma unroll 2
+    for (int k = 0; k < cb.n; ++k, a += lda, xin += xld) {
+      T2 av[4], xv[RPT];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) av[i] = rowOk[i] ? a[i] : mk2<T2>(0, 0);
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) xv[q] = colOk[q] ? xin[q] : mk2<T2>(0, 0);
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+          accr[i][q] += av[i].x * xv[q].x - av[i].y * xv[q].y;
+          acci[i][q] += av[i].x * xv[q].y + av[i].y * xv[q].x;
+        }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    if (!rowOk[i]) continue;
+#pragma unroll
+    for (int q = 0; q < RPT; ++q)
+      if (colOk[q]) W[(it.outRow + r0 + i) * R + c0 + q] = mk2<T2>(accr[i][q], acci[i][q]);
+  }
+}
+
+// R > 1: one CTA per (item, RHS tile of RT columns); 32 rows x RT outputs,
+// A and X staged through shared memory in chunks of KC columns.
 template <typename T2, int RT>
 __global__ void __launch_bounds__(256) applyTileKernel(
     ApplyItem const *__restrict__ items, ApplyContrib const *__restrict__ contribs,
@@ -634,6 +695,7 @@ __global__ void __launch_bounds__(256) applyTileKernel(
   }
 }
 
+
 template <typename T2>
 __global__ void applyReduceKernel(int32_t const *__restrict__ rowSeg,
                                   int64_t const *__restrict__ segStart,
@@ -669,6 +731,15 @@ __global__ void gatherRowsKernel(T2 const *X, int64_t ldx, int64_t const *perm,
     int64_t const i = e / R, r = e % R;
     out[e] = X[perm[i] * ldx + r];
   }
+}
+
+// BFG_APPLY_KERNEL=micro selects the register-blocked multi-RHS kernel
+int applyKernelVariant() {
+  static int v = [] {
+    char const *e = std::getenv("BFG_APPLY_KERNEL");
+    return (e && std::strcmp(e, "micro") == 0) ? 1 : 0;
+  }();
+  return v;
 }
 
 int gridFor(int64_t total, int threads) {
@@ -802,6 +873,16 @@ cudaError_t launchApplyStage(ApplyItem const *items, int64_t nItems,
   if (R == 1) {
     applyGemvKernel<T2><<<(unsigned)nItems, 32 * kGemvWarps, 0, stream>>>(items, contribs,
                                                                           arena, X, ldx, W);
+  } else if (applyKernelVariant() == 1) {
+    // register-blocked variant (kept for measurement)
+    dim3 grid((unsigned)((nItems + kMicroWarps - 1) / kMicroWarps),
+              (unsigned)(R <= 8 ? 1 : (R + 15) / 16));
+    if (R <= 8)
+      applyMicroKernel<T2, 2><<<grid, 32 * kMicroWarps, 0, stream>>>(items, nItems, contribs,
+                                                                    arena, X, ldx, W, R);
+    else
+      applyMicroKernel<T2, 4><<<grid, 32 * kMicroWarps, 0, stream>>>(items, nItems, contribs,
+                                                                    arena, X, ldx, W, R);
   } else if (R <= 8) {
     dim3 grid((unsigned)nItems, 1);
     applyTileKernel<T2, 8><<<grid, 256, 0, stream>>>(items, contribs, arena, X, ldx, W, R);

@@ -185,6 +185,61 @@ bfgStatus bfgHelm2KernelMatrix(bfgContext ctx, bfgHelm2 const *helm,
  * out[4i..4i+3] = J0, Y0, J1, Y1 at x[i] > 0 (host arrays). */
 bfgStatus bfgBessel01(bfgContext ctx, double const *x, int64_t n, double *out);
 
+/* ---------------------------------------------------------------------
+ * Boundary-integral systems and GMRES
+ * --------------------------------------------------------------------- */
+typedef struct bfgSystem_s *bfgSystem;
+
+/* A = diagShift I + (K + C) diag(w): the operator assembleButterfliedK
+ * builds (multiple_scattering_context.c:457-507; diagShift = 1/2 there).
+ * K is `fac`, built on the same points (original order) and layer
+ * potential as given here; C the Kapur-Rokhlin correction of order krOrder
+ * (2, 6, 10; 0 = none) inside each closed curve [curveOffsets[b],
+ * curveOffsets[b+1]) (bfQuadKrApplyBlockCorrectionTree, quadrature.c:222-269)
+ * with the reference's kernel callback (multiple_scattering_context.c:
+ * 27-42); w the quadrature weights.  `ctx` is the context of `fac`.
+ * Vectors of the system are in original point order. */
+bfgStatus bfgSystemCreate(bfgContext ctx, bfgFac fac, bfgHelm2 const *helm,
+                          double const *xy, double const *normals,
+                          double const *weights, int64_t const *curveOffsets,
+                          int64_t numCurves, int32_t krOrder, double diagShift,
+                          bfgSystem *sys);
+bfgStatus bfgSystemDestroy(bfgSystem sys);
+char const *bfgSystemGetErrorString(bfgSystem sys);
+/* Y = A X for one device complex128 vector (bfMatMul on the assembled
+ * operator). */
+bfgStatus bfgSystemApply(bfgSystem sys, void const *X, void *Y);
+/* Block-Jacobi preconditioner: dense diagonal block of A per curve, inverted
+ * on the GPU (assemblePreconditioner, multiple_scattering_context.c:545-634;
+ * the reference factors them with zgetrf, lu_dense_complex.c:185-232). */
+bfgStatus bfgSystemBuildBlockJacobi(bfgSystem sys);
+bfgStatus bfgSystemApplyBlockJacobi(bfgSystem sys, void const *R, void *Z);
+
+#define BFG_PRECOND_NONE 0
+#define BFG_PRECOND_BLOCK_JACOBI 1
+#define BFG_PRECOND_USER 2
+/* A right preconditioner z = M r on device complex128 vectors, launched on
+ * `cudaStream`; may change from call to call (flexible GMRES). */
+typedef bfgStatus (*bfgPrecondFn)(void *userData, void const *r, void *z, void *cudaStream);
+
+typedef struct bfgGmresResult {
+  int64_t iterations;
+  double relResidual;       /* |g_{j+1}| / ||b|| from the Arnoldi process */
+  double trueRelResidual;   /* ||b - A x|| / ||b|| recomputed at the end */
+  double seconds;           /* wall time of the solve */
+  int32_t converged;
+  int32_t reserved;
+} bfgGmresResult;
+
+/* Solves A x = b with right-preconditioned flexible GMRES (no restart, at
+ * most maxIter iterations), X holding x0 on entry and x on exit (device
+ * complex128).  Replaces bfSolveGMRES (linalg.c:47-317), which is
+ * left-preconditioned: here the convergence test |g_{j+1}|/||b|| < tol is
+ * on the true residual. */
+bfgStatus bfgSolveGmres(bfgSystem sys, void const *B, void *X, double tol,
+                        int64_t maxIter, int32_t precond, bfgPrecondFn userFn,
+                        void *userData, bfgGmresResult *result);
+
 /* Host-only (no GPU needed): the quadtrees and block structure that
  * bfgFacHelm2MakeMultilevel builds for the same inputs -- the permutations
  * and the plan text of bfgFacDescribe.  Either output may be NULL. */

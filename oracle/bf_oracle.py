@@ -943,6 +943,70 @@ def parse_plan(text: str):
     return rec()
 
 
+# Kapur-Rokhlin end-correction weights (quadrature.c:12-40; Kapur & Rokhlin,
+# SIAM J. Numer. Anal. 34 (1997))
+KR_WEIGHTS = {
+    2: [1.825748064736159, -1.325748064736159],
+    6: [4.967362978287758, -16.20501504859126, 25.85153761832639,
+        -22.22599466791883, 9.930104998037539, -1.817995878141594],
+    10: [7.832432020568779, -4.565161670374749, 1.452168846354677,
+         -2.901348302886379, 3.870862162579900, -3.523821383570681,
+         2.172421547519342, -8.707796087382991, 2.053584266072635,
+         -2.166984103403823],
+}
+
+
+def kernel_pairs(helm: Helm2, src, src_normals, tgt):
+    """bfHelm2GetKernelValue(helm, src_q, tgt_q, n_q, NULL) per pair q."""
+    src = np.ascontiguousarray(src, dtype=np.float64)
+    tgt = np.ascontiguousarray(tgt, dtype=np.float64)
+    nrm = np.ascontiguousarray(src_normals, dtype=np.float64)
+    out = np.empty(len(src), dtype=np.complex128)
+    cols = [np.ascontiguousarray(a) for a in (src[:, 0], src[:, 1], nrm[:, 0], nrm[:, 1],
+                                              tgt[:, 0], tgt[:, 1])]
+    rc = lib().oracle_kernel_pairs(
+        ctypes.c_int(helm.layer_pot), ctypes.c_double(helm.k),
+        ctypes.c_double(helm.alpha.real), ctypes.c_double(helm.alpha.imag),
+        ctypes.c_double(helm.beta.real), ctypes.c_double(helm.beta.imag),
+        *[_ptr(c) for c in cols], ctypes.c_int64(len(src)), _ptr(out))
+    if rc != 0:
+        raise NotImplementedError("layer potential %d" % helm.layer_pot)
+    return out
+
+
+def kr_correction(helm: Helm2, X, N, offsets, order: int):
+    """(rows, cols, vals) of the block KR correction (quadrature.c:124-164,
+    with K_helm2 of multiple_scattering_context.c:27-42: source x_i, normal
+    n_i, target x_j)."""
+    w = KR_WEIGHTS[order]
+    rows, cols, srcs, tgts = [], [], [], []
+    for b in range(len(offsets) - 1):
+        i0, i1 = offsets[b], offsets[b + 1]
+        m = i1 - i0
+        for i in range(i0, i1):
+            for p in range(order):
+                for j in (((i + p + 1 - i0) % m) + i0, (((i + m) - p - 1 - i0) % m) + i0):
+                    rows.append(i)
+                    cols.append(j)
+    rows = np.array(rows)
+    cols = np.array(cols)
+    vals = kernel_pairs(helm, X[rows], N[rows], X[cols])
+    weights = np.tile(np.repeat(np.array(w), 2), len(X))
+    return rows, cols, weights * vals
+
+
+def cfie_system_dense(helm: Helm2, X, N, W, offsets, order: int, shift: float = 0.5):
+    """Dense A = shift I + (K + C) diag(W) as assembleDenseK
+    (multiple_scattering_context.c:407-437) builds it."""
+    K = kernel_matrix(helm, X, X, N, None)
+    if order:
+        r, c, v = kr_correction(helm, X, N, offsets, order)
+        np.add.at(K, (r, c), v)
+    K = K * np.asarray(W)[None, :]
+    K[np.diag_indices(len(X))] += shift
+    return K
+
+
 def dense_rows(helm: Helm2, src_tree_pts, tgt_tree_pts, rows, X,
                src_normals=None, tgt_normals=None, chunk: int = 4096):
     """Rows ``rows`` (tree order) of K X with the dense FP64 kernel, in

@@ -62,6 +62,33 @@ void oracle_circle_points(double cx, double cy, double r, int64_t p,
   }
 }
 
+/* Point kernel bfHelm2GetKernelValue(helm, xsrc, xtgt, nsrc, NULL)
+ * (helm2.c:61-91) for q < count pairs (source q, target q); NaN at r == 0
+ * for the single layer, 0 for the double layer, as get_S_value /
+ * get_D_value (helm2.c:38-59). */
+int oracle_kernel_pairs(int layerPot, double k, double alphaRe, double alphaIm,
+                        double betaRe, double betaIm, double const *sx,
+                        double const *sy, double const *snx, double const *sny,
+                        double const *tx, double const *ty, int64_t count,
+                        cplx *out) {
+  cplx const alpha = alphaRe + I * alphaIm, beta = betaRe + I * betaIm;
+  for (int64_t q = 0; q < count; ++q) {
+    double r = hypot(tx[q] - sx[q], ty[q] - sy[q]);
+    cplx S = r == 0 ? NAN : I * (j0(k * r) + I * y0(k * r)) / 4;
+    cplx D = 0;
+    if (r >= 1e-15) {
+      double dot = snx[q] * (tx[q] - sx[q]) + sny[q] * (ty[q] - sy[q]);
+      cplx scale = (I / 4) * k * (j1(k * r) + I * y1(k * r)) / r;
+      D = scale * dot;
+    }
+    if (layerPot == LP_SINGLE) out[q] = S;
+    else if (layerPot == LP_PV_DOUBLE) out[q] = D;
+    else if (layerPot == LP_COMBINED_FIELD) out[q] = alpha * S + beta * D;
+    else return -1;
+  }
+  return 0;
+}
+
 /* K[i, j] for target i (tx, ty, tnx, tny) and source j (sx, sy, snx, sny).
  * Normal arrays may be NULL when the layer potential does not use them. */
 int oracle_kernel_matrix(int layerPot, double k, double alphaRe, double alphaIm,

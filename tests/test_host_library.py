@@ -18,7 +18,10 @@ from oracle import bf_oracle as O
 def declared_symbols():
     text = open(os.path.join(ROOT, "include", "bfg.h")).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(bfg[A-Z]\w*)\s*\(", text)))
+    text = "\n".join(ln for ln in text.split("\n") if not ln.lstrip().startswith("typedef"))
+    names = set(re.findall(r"\b(bfg[A-Z]\w*)\s*\(", text))
+    types = set(re.findall(r"\}\s*(bfg\w+)\s*;", open(os.path.join(ROOT, "include", "bfg.h")).read()))
+    return sorted(names - types - {"bfgStatus"})
 
 
 def test_library_exports_every_declared_symbol():
