@@ -433,6 +433,54 @@ bfgStatus applyDispatch(bfgFac f, bfgPrecision prec, void const *X, int64_t ldx,
 
 }  // namespace
 
+// Support of bfgFacApplyNoAlloc (bfg_noalloc.cu): the FP64 apply with a
+// workspace the caller provides, so that nothing is allocated.
+namespace bfg {
+
+int64_t noAllocWorkspaceEntries(bfgFac f, int64_t R, uint32_t flags) {
+  int64_t e = std::max<int64_t>(1, f->prog.wsRows) * R;
+  if (flags & BFG_APPLY_ORIGINAL_ORDER) e += f->prog.numCols * R;
+  return e;
+}
+
+int noAllocDevice(bfgFac f) { return f->ctx->device; }
+
+bfgStatus noAllocFail(bfgFac f, bfgStatus st, char const *msg) { return fail(f->ctx, st, msg); }
+
+bfgStatus noAllocApplyFp64(bfgFac f, double2 const *X, int64_t ldx, int64_t R, double2 *Y,
+                           int64_t ldy, uint32_t flags, double2 *scratch) {
+  return guarded(f->ctx, [&]() -> bfgStatus {
+    cudaStream_t s = f->ctx->stream;
+    bfg::ApplyProgram const &p = f->prog;
+    double2 *W = scratch;
+    double2 const *Xt = X;
+    int64_t ldxt = ldx;
+    if (flags & BFG_APPLY_ORIGINAL_ORDER) {
+      double2 *xg = scratch + std::max<int64_t>(1, p.wsRows) * R;
+      ck(bfg::launchGatherRows<double2>(X, ldx, f->srcPerm.as<int64_t>(), p.numCols, R, xg, s),
+         "gather");
+      Xt = xg;
+      ldxt = R;
+    }
+    size_t const nStages = f->stageItem0.size() - 1;
+    for (size_t st = 0; st < nStages; ++st) {
+      int64_t a = f->stageItem0[st], b = f->stageItem0[st + 1];
+      ck(bfg::launchApplyStage<double2>(f->items.as<bfg::ApplyItem>() + a, b - a,
+                                        f->contribs.as<bfg::ApplyContrib>(),
+                                        f->arena64.as<double2>(), Xt, ldxt, W, R, s),
+         "apply stage");
+    }
+    ck(bfg::launchApplyReduce<double2>(
+           f->rowSeg.as<int32_t>(), f->segStart.as<int64_t>(), f->segContrib0.as<int64_t>(),
+           f->segBase.as<int64_t>(), W, R, Y, ldy, p.numRows,
+           (flags & BFG_APPLY_ORIGINAL_ORDER) ? f->tgtPerm.as<int64_t>() : nullptr, s),
+       "apply reduce");
+    return BFG_OK;
+  });
+}
+
+}  // namespace bfg
+
 extern "C" {
 
 bfgStatus bfgContextCreate(int32_t device, bfgContext *out) {

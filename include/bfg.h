@@ -151,6 +151,19 @@ bfgStatus bfgFacApplyHost(bfgFac fac, bfgPrecision precision, double const *X,
                           int64_t ldx, int64_t numRhs, double *Y, int64_t ldy,
                           uint32_t flags);
 
+/* No counterpart in the reference.  The FP64 product of bfgFacApply (device
+ * complex128 X and Y, same flags and contract) for callers that cannot
+ * allocate GPU memory -- their device memory is reserved up front by another
+ * allocator, or cudaMalloc's possible device synchronisation is not
+ * acceptable on their path.  The workspace is a static 32 MiB device array
+ * inside the library (held by every GPU that loads it); calls whose
+ * workspace would exceed it fail with BFG_ERROR_OUT_OF_RANGE.  The first
+ * call on a device looks up the array's address and should come before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race. */
+bfgStatus bfgFacApplyNoAlloc(bfgFac fac, void const *X, int64_t ldx, int64_t numRhs,
+                             void *Y, int64_t ldy, uint32_t flags);
+
 /* bfgFacApply with a CUDA event around every launch; launchMs[i] receives
  * the device time of launch i (stages in order, then the final sum).
  * Synchronises. */
