@@ -1,7 +1,7 @@
 """Benchmark of the butterfly Helmholtz apply on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl bfg|reference]
-                    [--config c4|c2|c1] [--rhs R]
+                    [--config c4|c2|c2s|c1] [--rhs R]
 
 One step = one apply of the factorization to R right-hand sides (the
 workload's synthetic, seeded inputs).  The metric is right-hand sides per
@@ -37,17 +37,26 @@ CONFIGS = {
     "c1": dict(n=4096, k=64.0, curve="circle", a=3.0, b=3.0, leaf=64, tol=1e-8, R=1),
     # 65,536 / ellipse (3,2), k=512, tol 1e-10, 16 RHS
     "c2": dict(n=65536, k=512.0, curve="ellipse", a=3.0, b=2.0, leaf=64, tol=1e-10, R=16),
+    # the c2 geometry at 32,768 points and k=256 (kernel profiles: the FP32
+    # arena, 0.5 GB, is still larger than L2)
+    "c2s": dict(n=32768, k=256.0, curve="ellipse", a=3.0, b=2.0, leaf=64, tol=1e-10, R=16),
     # 262,144 / star r = 3 + 0.5 cos 5 theta, k=2048, tol 1e-7, 256 RHS
     "c4": dict(n=262144, k=2048.0, curve="star", a=3.0, b=3.0, leaf=64, tol=1e-7, R=256),
 }
 METRIC = "Butterfly apply RHS/s at 1e-6 rel err vs plain FP64 GPU; GMRES time-to-1e-8"
+# DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
+# byte of each stage launch of the FP32 16-RHS apply, from one ncu capture of
+# the c2s workload; the c2 workload (same geometry, kernel and stage
+# structure at twice the size) reports its dominant launch's traffic as this
+# ratio times its own algorithmic bytes
+NCU_DRAM_PER_ALG = {("fp32", 16, 5): [0.7973, 1.0266, 0.9855, 0.7925]}
 ERR_BOUND = 1e-6
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="bfg", choices=["bfg", "reference"])
     ap.add_argument("--config", default=os.environ.get("BFG_BENCH_CONFIG", "c2"),
@@ -335,8 +344,15 @@ def main():
     except (OSError, KeyError, ValueError):
         peak, peak_src = 6800.0, "fallback"
     achieved = float(alg_bytes / (per[dom] / 1e3) / 1e9)
+    ratios = NCU_DRAM_PER_ALG.get((head, R, len(per)))
+    traffic, traffic_src = None, None
+    if ratios is not None and args.config in ("c2", "c2s") and dom < len(ratios):
+        traffic = float(ratios[dom] * alg_bytes)
+        traffic_src = ("ncu DRAM bytes of the same stage in the c2s capture, scaled by "
+                       "algorithmic bytes" if args.config == "c2" else "ncu capture")
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
+            "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
+            "peak_source": peak_src,
             "kernel": "apply launch %d of %d" % (dom, len(per)),
             "launch_ms": float(per[dom]), "alg_bytes": alg_bytes,
             "launch_share": launch_share,

@@ -84,6 +84,8 @@ def lib() -> ctypes.CDLL:
         "bfgFacOptionsDefault": [ctypes.POINTER(_FacOptionsC)],
         "bfgFacHelm2MakeMultilevel": [_VP, ctypes.POINTER(_Helm2C), _VP, _VP, _I64, _VP, _VP,
                                       _I64, ctypes.POINTER(_FacOptionsC), ctypes.POINTER(_VP)],
+        "bfgFacHelm2MakeBatched": [_VP, ctypes.POINTER(_Helm2C), _VP, _I64, _VP, _VP, _VP, _VP,
+                                   _VP, _VP, ctypes.POINTER(_FacOptionsC), ctypes.POINTER(_VP)],
         "bfgFacDestroy": [_VP],
         "bfgFacGetShape": [_VP, ctypes.POINTER(_I64), ctypes.POINTER(_I64)],
         "bfgFacGetPerms": [_VP, _VP, _VP],
@@ -275,6 +277,43 @@ class FacHelm2:
             ctx.handle, ctypes.byref(hc), _ptr(src), _ptr(sn), len(src), _ptr(tgt), _ptr(tn),
             len(tgt), ctypes.byref(opts), ctypes.byref(h)), "make_multilevel")
         return Fac(ctx, h, helm)
+
+
+def make_batched(helm: Helm2, problems, ks, *, leaf_size: int = 1, rank_eps: float = 1e-15,
+                 pinv_tol: float | None = None, context: Context | None = None) -> "Fac":
+    """Factorize many independent problems in one go (bfgFacHelm2MakeBatched).
+    ``problems``: list of (src, tgt) or (src, tgt, src_normals, tgt_normals);
+    ``ks``: wavenumber per problem.  The result applies diag(A_0, ..., A_P-1);
+    ``fac.src_offsets`` / ``fac.tgt_offsets`` locate each problem's rows."""
+    ctx = context or default_context()
+    srcs = [_xy(p[0]) for p in problems]
+    tgts = [_xy(p[1]) for p in problems]
+    sn = [_xy(p[2]) if len(p) > 2 and p[2] is not None else None for p in problems]
+    tn = [_xy(p[3]) if len(p) > 3 and p[3] is not None else None for p in problems]
+    so = np.concatenate([[0], np.cumsum([len(a) for a in srcs])]).astype(np.int64)
+    to = np.concatenate([[0], np.cumsum([len(a) for a in tgts])]).astype(np.int64)
+    src = np.ascontiguousarray(np.concatenate(srcs))
+    tgt = np.ascontiguousarray(np.concatenate(tgts))
+    snc = None if any(a is None for a in sn) else np.ascontiguousarray(np.concatenate(sn))
+    tnc = None if any(a is None for a in tn) else np.ascontiguousarray(np.concatenate(tn))
+    kk = np.ascontiguousarray(ks, dtype=np.float64)
+    if len(kk) != len(problems):
+        raise ValueError("one wavenumber per problem")
+    opts = _FacOptionsC()
+    lib().bfgFacOptionsDefault(ctypes.byref(opts))
+    opts.leafSize = int(leaf_size)
+    opts.rankEps = float(rank_eps)
+    if pinv_tol is not None:
+        opts.pinvCut, opts.pinvTol = 1, float(pinv_tol)
+    h = _VP()
+    hc = helm._c()
+    ctx.check(lib().bfgFacHelm2MakeBatched(ctx.handle, ctypes.byref(hc), _ptr(kk), len(kk),
+                                           _ptr(src), _ptr(snc), _ptr(so), _ptr(tgt), _ptr(tnc),
+                                           _ptr(to), ctypes.byref(opts), ctypes.byref(h)),
+              "make_batched")
+    fac = Fac(ctx, h, helm)
+    fac.src_offsets, fac.tgt_offsets = so, to
+    return fac
 
 
 class Fac:

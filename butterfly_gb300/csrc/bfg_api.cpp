@@ -172,6 +172,7 @@ bfg::FillDesc toDesc(bfg::Block const &b) {
   d.corig[0] = b.corig.cx; d.corig[1] = b.corig.cy; d.corig[2] = b.corig.r;
   d.ceq[0] = b.ceq.cx; d.ceq[1] = b.ceq.cy; d.ceq[2] = b.ceq.r;
   d.cchk[0] = b.cchk.cx; d.cchk[1] = b.cchk.cy; d.cchk[2] = b.cchk.r;
+  d.k = b.k;
   return d;
 }
 
@@ -594,6 +595,74 @@ bfgStatus bfgFacHelm2MakeMultilevel(bfgContext ctx, bfgHelm2 const *helm, double
     } catch (std::runtime_error const &e) {
       delete f;
       return fail(ctx, BFG_ERROR_RUNTIME, std::string("make: ") + e.what());
+    } catch (...) {
+      delete f;
+      throw;
+    }
+    *out = f;
+    return BFG_OK;
+  });
+}
+
+bfgStatus bfgFacHelm2MakeBatched(bfgContext ctx, bfgHelm2 const *helm, double const *k,
+                                 int64_t numProblems, double const *srcXy,
+                                 double const *srcNormals, int64_t const *srcOffsets,
+                                 double const *tgtXy, double const *tgtNormals,
+                                 int64_t const *tgtOffsets, bfgFacOptions const *opts,
+                                 bfgFac *out) {
+  if (!ctx) return BFG_ERROR_INVALID_ARGUMENTS;
+  return guarded(ctx, [&]() -> bfgStatus {
+    if (!helm || !k || !srcXy || !tgtXy || !srcOffsets || !tgtOffsets || !out || numProblems < 1)
+      return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "batched make: null argument");
+    *out = nullptr;
+    if (!validLayerPot(helm->layerPot))
+      return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "batched make: unknown layer potential");
+    if (srcOffsets[0] != 0 || tgtOffsets[0] != 0)
+      return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "batched make: offsets must start at 0");
+    for (int64_t p = 0; p < numProblems; ++p) {
+      if (!(k[p] > 0) || srcOffsets[p + 1] <= srcOffsets[p] || tgtOffsets[p + 1] <= tgtOffsets[p])
+        return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS,
+                    "batched make: every problem needs k > 0 and points");
+    }
+    bool const needSrcN = helm->layerPot == bfg::kLpPvDouble ||
+                          helm->layerPot == bfg::kLpCombinedField;
+    bool const needTgtN = helm->layerPot == bfg::kLpPvNormalDerivSingle;
+    if ((needSrcN && !srcNormals) || (needTgtN && !tgtNormals))
+      return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "batched make: normals needed");
+    int64_t const nSrc = srcOffsets[numProblems], nTgt = tgtOffsets[numProblems];
+    for (int64_t i = 0; i < 2 * nSrc; ++i)
+      if (!std::isfinite(srcXy[i])) return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "batched make: non-finite point");
+    for (int64_t i = 0; i < 2 * nTgt; ++i)
+      if (!std::isfinite(tgtXy[i])) return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "batched make: non-finite point");
+    bfgFacOptions o;
+    bfgFacOptionsDefault(&o);
+    if (opts) o = *opts;
+    if (o.leafSize < 1 || !(o.rankEps > 0 && o.rankEps < 1) || (o.pinvCut != 0 && o.pinvCut != 1) ||
+        (o.pinvCut == 1 && !(o.pinvTol > 0 && o.pinvTol < 1)))
+      return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "batched make: bad options");
+    auto *f = new bfgFac_s;
+    f->ctx = ctx;
+    f->helm = *helm;
+    f->helm.k = k[0];
+    f->opts = o;
+    try {
+      bfg::PlanParams pp;
+      pp.leafSize = o.leafSize;
+      pp.rankEps = o.rankEps;
+      bfg::makePlanBatched(f->plan, pp, k, srcXy, srcOffsets, tgtXy, tgtOffsets, numProblems);
+      cudaStream_t s = ctx->stream;
+      f->srcHasNormals = srcNormals != nullptr;
+      f->tgtHasNormals = tgtNormals != nullptr;
+      uploadTreePoints(f->srcPts, srcXy, srcNormals, nSrc, f->plan.src.perm, s);
+      uploadTreePoints(f->tgtPts, tgtXy, tgtNormals, nTgt, f->plan.tgt.perm, s);
+      upload(f->srcPerm, f->plan.src.perm, s, "perm");
+      upload(f->tgtPerm, f->plan.tgt.perm, s, "perm");
+      factorize(f);
+      buildApply(f);
+      fillStats(f);
+    } catch (std::runtime_error const &e) {
+      delete f;
+      return fail(ctx, BFG_ERROR_RUNTIME, std::string("batched make: ") + e.what());
     } catch (...) {
       delete f;
       throw;

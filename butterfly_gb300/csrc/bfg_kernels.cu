@@ -87,6 +87,7 @@ __global__ void fillBlocksKernel(FillDesc const *__restrict__ descs, PointsDev s
                                  int32_t *status) {
   extern __shared__ double proxy[];   // 4 * n for LAST blocks
   FillDesc const d = descs[blockIdx.x];
+  kp.k = d.k;
   int const m = d.m, n = d.n;
   double2 *out = arena + d.arenaOff;
   bool const useSrcN = kp.layerPot == kLpPvDouble || kp.layerPot == kLpCombinedField;
@@ -168,6 +169,7 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
   int const blk = kMode == 2 ? (int)(blockIdx.x / kClusterCtas) : (int)blockIdx.x;
   int const rank = kMode == 2 ? (int)(blockIdx.x % kClusterCtas) : 0;
   FillDesc const d = descs[blk];
+  kp.k = d.k;
   int const p = d.m, n = d.n, LD = 2 * p;
   int const tid = threadIdx.x, nthr = blockDim.x;
   int const lane = tid & 31, warp = tid >> 5, nWarps = nthr >> 5;
@@ -569,67 +571,156 @@ applyGemvKernel(ApplyItem const *__restrict__ items, ApplyContrib const *__restr
   }
 }
 
-// R > 1: one CTA per (item, RHS tile of RT columns); 32 rows x RT outputs,
-// K staged through shared memory in chunks of KC columns.
-// R > 1, register-blocked: one warp per (item, RHS tile of 4*RPT columns);
-// lane -> 4 consecutive rows x RPT consecutive RHS (8 row groups x 4 RHS
-// groups), operands read straight from global memory (the 8 lanes that share
-// a row group, and the 8 that share an RHS group, hit the same L1 lines).
-// Each column k costs 4 + RPT loads for 4*RPT complex MACs per lane.
-constexpr int kMicroWarps = 4;
+// two adjacent complex values from shared memory (16-byte aligned)
+__device__ __forceinline__ void load2(float2 const *p, float2 &a, float2 &b) {
+  float4 const v = *reinterpret_cast<float4 const *>(p);
+  a = make_float2(v.x, v.y);
+  b = make_float2(v.z, v.w);
+}
+__device__ __forceinline__ void load2(double2 const *p, double2 &a, double2 &b) {
+  a = p[0];
+  b = p[1];
+}
 
-template <typename T2, int RPT>
-__global__ void __launch_bounds__(32 * kMicroWarps) applyMicroKernel(
-    ApplyItem const *__restrict__ items, int64_t nItems,
-    ApplyContrib const *__restrict__ contribs, T2 const *__restrict__ arena,
-    T2 const *__restrict__ X, int64_t ldx, T2 *__restrict__ W, int64_t R) {
+// Asynchronous global -> shared copies (LDGSTS) of one complex entry; the
+// 16-byte form bypasses L1 (stored blocks are read once per launch).
+__device__ __forceinline__ void cpAsyncEntry(float2 *dst, float2 const *src) {
+  unsigned const d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpAsyncEntry(double2 *dst, double2 const *src) {
+  unsigned const d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpAsyncCommit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpAsyncWait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// R > 1, pipelined: one CTA of NW warps per (item, tile of 16 RHS).  The
+// item's contributions are walked in chunks of up to KC columns; each chunk's
+// A panel (rows x columns) and X panel (columns x 16 RHS) are copied into
+// shared memory with cp.async, one chunk ahead of the one being multiplied,
+// so every load of a chunk is in flight at once instead of one column per
+// round trip.  Warp w multiplies the columns w, w+NW, ... of each chunk; a
+// lane owns 4 rows x 4 RHS of the 32 x 16 tile (4 vector shared loads per
+// 16 complex MACs) in 16 register accumulators; the NW partial 32 x 16 tiles
+// are summed in shared memory in a fixed order.  Rows >= item rows and RHS
+// >= R are never copied: they only reach accumulators that are not stored.
+template <typename T2>
+struct PipeShape {
+  static constexpr int KC = 32;   // 12 KB (FP32) / 24 KB (FP64) per stage
+  static constexpr int RT = 16;
+  static constexpr size_t stageBytes = (size_t)KC * (32 + RT) * sizeof(T2);
+};
+constexpr int kPipeWarps = 4;
+
+template <typename T2, int NW, int S>
+__global__ void __launch_bounds__(32 * NW, sizeof(T2) == 8 ? 8 : 4) applyPipeKernel(
+    ApplyItem const *__restrict__ items, ApplyContrib const *__restrict__ contribs,
+    T2 const *__restrict__ arena, T2 const *__restrict__ X, int64_t ldx,
+    T2 *__restrict__ W, int64_t R) {
   using T = typename Real<T2>::T;
-  int64_t const item = (int64_t)blockIdx.x * kMicroWarps + (threadIdx.x >> 5);
-  if (item >= nItems) return;
-  int const lane = threadIdx.x & 31;
-  int const rg = lane & 7, cg = lane >> 3;
-  ApplyItem const it = items[item];
-  int const r0 = rg * 4;
-  int64_t const c0 = (int64_t)blockIdx.y * (4 * RPT) + cg * RPT;
-  bool rowOk[4];
+  constexpr int KC = PipeShape<T2>::KC, RT = PipeShape<T2>::RT, TH = 32 * NW;
+  static_assert((size_t)NW * RT * 32 <= (size_t)S * KC * 32, "partials must fit in sA");
+  extern __shared__ __align__(16) unsigned char pipeSmem[];
+  T2 *const sA = reinterpret_cast<T2 *>(pipeSmem);   // [S][KC][32]
+  T2 *const sX = sA + S * KC * 32;                   // [S][KC][RT]
+  int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int const rg = lane & 7, cg = lane >> 3;   // lane's rows 4rg.., RHS 4cg..
+  ApplyItem const it = items[blockIdx.x];
+  int64_t const r0 = (int64_t)blockIdx.y * RT;
+  int const nr = (R - r0) < RT ? (int)(R - r0) : RT;
+  int const rows = it.rows;
+
+  // issue cursor over (contribution, first column); uniform across the CTA
+  int ci = 0, cj = 0;
+  ApplyContrib icb{};
+  if (it.nContrib > 0) icb = contribs[it.contrib0];
+  int ncBuf[S];
+  int issued = 0;
+  // copies the next chunk (if any) into stage `slot`, then commits a group
+  // (an empty one at the end, so that group counts stay in step)
+  auto tryIssue = [&](int slot) {
+    if (ci < it.nContrib) {
+      int const nc = min(KC, icb.n - cj);
+      T2 const *a = arena + icb.aOff + (int64_t)cj * icb.lda;
+      int64_t const lda = icb.lda;
+      for (int e = threadIdx.x; e < nc * 32; e += TH) {
+        int const col = e >> 5, row = e & 31;
+        if (row < rows) cpAsyncEntry(&sA[(slot * KC + col) * 32 + row], a + col * lda + row);
+      }
+      int64_t const xld = icb.inIsX ? ldx : R;
+      T2 const *x =
+          (icb.inIsX ? X + icb.inRow * ldx : W + icb.inRow * R) + r0 + (int64_t)cj * xld;
+      for (int e = threadIdx.x; e < nc * RT; e += TH) {
+        int const col = e / RT, q = e % RT;
+        if (q < nr) cpAsyncEntry(&sX[(slot * KC + col) * RT + q], x + col * xld + q);
+      }
+      ncBuf[slot] = nc;
+      ++issued;
+      cj += nc;
+      if (cj >= icb.n) {
+        ++ci;
+        cj = 0;
+        if (ci < it.nContrib) icb = contribs[it.contrib0 + ci];
+      }
+    }
+    cpAsyncCommit();
+  };
+
+  T accr[RT], acci[RT];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) rowOk[q] = r0 + q < it.rows;
-  bool colOk[RPT];
+  for (int q = 0; q < RT; ++q) accr[q] = acci[q] = 0;
+
 #pragma unroll
-  for (int q = 0; q < RPT; ++q) colOk[q] = c0 + q < R;
-  T accr[4][RPT], acci[4][RPT];
+  for (int sl = 0; sl < S - 1; ++sl) tryIssue(sl);
+  for (int i = 0; i < issued; ++i) {
+    tryIssue((i + S - 1) % S);   // the stage multiplied in the previous pass
+    cpAsyncWait<S - 1>();         // chunk i has landed
+    __syncthreads();
+    int const slot = i % S;
+    int const nc = ncBuf[slot];
+    T2 const *pa = sA + slot * KC * 32 + 4 * rg;
+    T2 const *px = sX + slot * KC * RT + 4 * cg;
+    for (int col = warp; col < nc; col += NW) {
+      T2 a[4], x[4];
+      load2(pa + col * 32, a[0], a[1]);
+      load2(pa + col * 32 + 2, a[2], a[3]);
+      load2(px + col * RT, x[0], x[1]);
+      load2(px + col * RT + 2, x[2], x[3]);
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+      for (int u = 0; u < 4; ++u)
 #pragma unroll
-    for (int q = 0; q < RPT; ++q) accr[i][q] = acci[i][q] = 0;
-  for (int cbi = 0; cbi < it.nContrib; ++cbi) {
-    ApplyContrib const cb = contribs[it.contrib0 + cbi];
-    T2 const *a = arena + cb.aOff + r0;
-    T2 const *xin = (cb.inIsX ? X + cb.inRow * ldx : W + cb.inRow * R) + c0;
-    int64_t const xld = cb.inIsX ? ldx : R;
-    int64_t const lda = cb.lda;
-#pragma unroll 2
-    for (int k = 0; k < cb.n; ++k, a += lda, xin += xld) {
-      T2 av[4], xv[RPT];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) av[i] = rowOk[i] ? a[i] : mk2<T2>(0, 0);
-#pragma unroll
-      for (int q = 0; q < RPT; ++q) xv[q] = colOk[q] ? xin[q] : mk2<T2>(0, 0);
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int q = 0; q < RPT; ++q) {
-          accr[i][q] += av[i].x * xv[q].x - av[i].y * xv[q].y;
-          acci[i][q] += av[i].x * xv[q].y + av[i].y * xv[q].x;
+        for (int q = 0; q < 4; ++q) {
+          accr[4 * u + q] += a[u].x * x[q].x - a[u].y * x[q].y;
+          acci[4 * u + q] += a[u].x * x[q].y + a[u].y * x[q].x;
         }
     }
+    __syncthreads();
   }
+  cpAsyncWait<0>();
+
+  T2 *const part = sA;   // [NW][RT][32], reuses the drained stage buffers
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    if (!rowOk[i]) continue;
+  for (int u = 0; u < 4; ++u)
 #pragma unroll
-    for (int q = 0; q < RPT; ++q)
-      if (colOk[q]) W[(it.outRow + r0 + i) * R + c0 + q] = mk2<T2>(accr[i][q], acci[i][q]);
+    for (int q = 0; q < 4; ++q)
+      part[(warp * RT + 4 * cg + q) * 32 + 4 * rg + u] =
+          mk2<T2>(accr[4 * u + q], acci[4 * u + q]);
+  __syncthreads();
+  for (int e = threadIdx.x; e < 32 * RT; e += TH) {
+    int const row = e & 31, q = e >> 5;
+    if (row >= rows || q >= nr) continue;
+    T sr = 0, si = 0;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      T2 const v = part[(w * RT + q) * 32 + row];
+      sr += v.x;
+      si += v.y;
+    }
+    W[(it.outRow + row) * R + r0 + q] = mk2<T2>(sr, si);
   }
 }
 
@@ -733,11 +824,14 @@ __global__ void gatherRowsKernel(T2 const *X, int64_t ldx, int64_t const *perm,
   }
 }
 
-// BFG_APPLY_KERNEL=micro selects the register-blocked multi-RHS kernel
-int applyKernelVariant() {
-  static int v = [] {
+// Multi-RHS kernel choice: the pipelined kernel above 8 RHS, the shared-memory
+// tile kernel up to 8 (the pipelined kernel computes 16 RHS per CTA); the
+// environment variable BFG_APPLY_KERNEL=tile forces the tile kernel for every
+// R > 1 (for A/B measurements).
+bool forceTileKernel() {
+  static bool v = [] {
     char const *e = std::getenv("BFG_APPLY_KERNEL");
-    return (e && std::strcmp(e, "micro") == 0) ? 1 : 0;
+    return e && std::strcmp(e, "tile") == 0;
   }();
   return v;
 }
@@ -873,16 +967,14 @@ cudaError_t launchApplyStage(ApplyItem const *items, int64_t nItems,
   if (R == 1) {
     applyGemvKernel<T2><<<(unsigned)nItems, 32 * kGemvWarps, 0, stream>>>(items, contribs,
                                                                           arena, X, ldx, W);
-  } else if (applyKernelVariant() == 1) {
-    // register-blocked variant (kept for measurement)
-    dim3 grid((unsigned)((nItems + kMicroWarps - 1) / kMicroWarps),
-              (unsigned)(R <= 8 ? 1 : (R + 15) / 16));
-    if (R <= 8)
-      applyMicroKernel<T2, 2><<<grid, 32 * kMicroWarps, 0, stream>>>(items, nItems, contribs,
-                                                                    arena, X, ldx, W, R);
-    else
-      applyMicroKernel<T2, 4><<<grid, 32 * kMicroWarps, 0, stream>>>(items, nItems, contribs,
-                                                                    arena, X, ldx, W, R);
+  } else if (R > 8 && !forceTileKernel()) {
+    size_t const smem = 2 * PipeShape<T2>::stageBytes;
+    cudaError_t e = cudaFuncSetAttribute(applyPipeKernel<T2, kPipeWarps, 2>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((unsigned)nItems, (unsigned)((R + 15) / 16));
+    applyPipeKernel<T2, kPipeWarps, 2><<<grid, 32 * kPipeWarps, smem, stream>>>(
+        items, contribs, arena, X, ldx, W, R);
   } else if (R <= 8) {
     dim3 grid((unsigned)nItems, 1);
     applyTileKernel<T2, 8><<<grid, 256, 0, stream>>>(items, contribs, arena, X, ldx, W, R);

@@ -15,6 +15,8 @@
 #include "bfg_plan.hpp"
 
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <cmath>
 #include <cstdio>
 #include <map>
@@ -485,6 +487,74 @@ void makePlan(Plan &plan, PlanParams const &params, double const *srcXy,
   }
   if (plan.blockOrder.size() != plan.blocks.size())
     throw std::runtime_error("plan traversal lost blocks");
+  for (auto &b : plan.blocks) b.k = params.k;
+  plan.roots.assign(1, Plan::Root{plan.root, 0, 0});
+  int64_t off = 0;
+  for (int32_t bi : plan.blockOrder) {
+    plan.blocks[bi].arenaOff = off;
+    off += (int64_t)plan.blocks[bi].m * plan.blocks[bi].n;
+  }
+  plan.arenaEntries = off;
+}
+
+void makePlanBatched(Plan &plan, PlanParams const &params, double const *k,
+                     double const *srcXy, int64_t const *srcOff, double const *tgtXy,
+                     int64_t const *tgtOff, int64_t numProblems) {
+  if (numProblems < 1) throw std::runtime_error("no problems");
+  std::vector<Plan> subs((size_t)numProblems);
+  std::vector<std::string> errs((size_t)numProblems);
+  unsigned nthreads = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), 32u));
+  std::atomic<int64_t> next{0};
+  auto worker = [&]() {
+    for (int64_t p; (p = next++) < numProblems;) {
+      try {
+        PlanParams pp = params;
+        pp.k = k[p];
+        makePlan(subs[(size_t)p], pp, srcXy + 2 * srcOff[p], srcOff[p + 1] - srcOff[p],
+                 tgtXy + 2 * tgtOff[p], tgtOff[p + 1] - tgtOff[p]);
+      } catch (std::exception const &e) {
+        errs[(size_t)p] = e.what();
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (unsigned t = 0; t < nthreads; ++t) pool.emplace_back(worker);
+  for (auto &t : pool) t.join();
+  for (int64_t p = 0; p < numProblems; ++p)
+    if (!errs[(size_t)p].empty())
+      throw std::runtime_error("problem " + std::to_string(p) + ": " + errs[(size_t)p]);
+
+  plan = Plan();
+  for (int64_t p = 0; p < numProblems; ++p) {
+    Plan const &q = subs[(size_t)p];
+    int32_t const bBase = (int32_t)plan.blocks.size(), fBase = (int32_t)plan.factors.size();
+    int32_t const prBase = (int32_t)plan.products.size(), nBase = (int32_t)plan.pnodes.size();
+    int64_t const sB = srcOff[p], tB = tgtOff[p];
+    for (Block b : q.blocks) {
+      b.s0 += sB; b.s1 += sB; b.t0 += tB; b.t1 += tB;
+      plan.blocks.push_back(b);
+    }
+    for (Factor f : q.factors) {
+      for (auto &bi : f.blocks) bi += bBase;
+      plan.factors.push_back(std::move(f));
+    }
+    for (Product pr : q.products) {
+      for (auto &fi : pr.factors) fi += fBase;
+      pr.t0 += tB; pr.t1 += tB; pr.s0 += sB; pr.s1 += sB;
+      plan.products.push_back(std::move(pr));
+    }
+    for (PNode nd : q.pnodes) {
+      for (auto &c : nd.children) c += nBase;
+      if (nd.product >= 0) nd.product += prBase;
+      if (nd.block >= 0) nd.block += bBase;
+      plan.pnodes.push_back(std::move(nd));
+    }
+    for (int32_t bi : q.blockOrder) plan.blockOrder.push_back(bi + bBase);
+    plan.roots.push_back(Plan::Root{q.root + nBase, tB, sB});
+    for (int64_t v : q.src.perm) plan.src.perm.push_back(v + sB);
+    for (int64_t v : q.tgt.perm) plan.tgt.perm.push_back(v + tB);
+  }
+  plan.root = plan.roots[0].pnode;
   int64_t off = 0;
   for (int32_t bi : plan.blockOrder) {
     plan.blocks[bi].arenaOff = off;
@@ -496,14 +566,21 @@ void makePlan(Plan &plan, PlanParams const &params, double const *srcXy,
 std::string Plan::text() const {
   std::string out;
   char buf[128];
-  std::vector<int32_t> stack{root};
-  // iterative pre-order walk that emits children in order
+  // iterative pre-order walk that emits children in order; a batch of
+  // problems prints each one after a "PROBLEM p" line
   struct Frame { int32_t kind; int32_t idx; };
-  std::vector<Frame> st{{0, root}};
+  std::vector<Frame> st;
+  for (size_t r = roots.size(); r-- > 0;) {
+    st.push_back({0, roots[r].pnode});
+    if (roots.size() > 1) st.push_back({2, (int32_t)r});
+  }
   while (!st.empty()) {
     Frame fr = st.back();
     st.pop_back();
-    if (fr.kind == 0) {
+    if (fr.kind == 2) {
+      std::snprintf(buf, sizeof buf, "PROBLEM %d\n", fr.idx);
+      out += buf;
+    } else if (fr.kind == 0) {
       PNode const &nd = pnodes[fr.idx];
       if (nd.type == 0) {
         std::snprintf(buf, sizeof buf, "BD %d %d\n", nd.nr, nd.nc);
@@ -594,7 +671,9 @@ void makeApplyProgram(Plan const &plan, ApplyProgram &prog) {
   };
 
   // walk the HODBF in plan order, assigning workspace regions
-  std::vector<std::pair<int32_t, std::pair<int64_t, int64_t>>> st{{plan.root, {0, 0}}};
+  std::vector<std::pair<int32_t, std::pair<int64_t, int64_t>>> st;
+  for (size_t r = plan.roots.size(); r-- > 0;)
+    st.push_back({plan.roots[r].pnode, {plan.roots[r].rowBase, plan.roots[r].colBase}});
   // (pnode, (rowBase, colBase)) -- rowBase/colBase are absolute tree offsets
   std::vector<std::pair<int32_t, std::pair<int64_t, int64_t>>> order;
   while (!st.empty()) {
@@ -664,10 +743,23 @@ void makeApplyProgram(Plan const &plan, ApplyProgram &prog) {
   prog.wsRows = ws;
   prog.flopsPerRhs = flops;
 
-  // flatten stages
+  // flatten stages, each in decreasing order of work (rows x columns): the
+  // GPU starts CTAs in launch order, so the longest items start first and the
+  // short ones fill in behind them.  Items write disjoint rows, so the order
+  // changes no result.
   prog.stageItem0.push_back(0);
   for (size_t s = 0; s < stItems.size(); ++s) {
+    std::vector<int64_t> work(stItems[s].size());
     for (size_t k = 0; k < stItems[s].size(); ++k) {
+      int64_t cols = 0;
+      for (auto const &c : stContribs[s][k]) cols += c.n;
+      work[k] = cols * stItems[s][k].rows;
+    }
+    std::vector<size_t> idx(stItems[s].size());
+    for (size_t k = 0; k < idx.size(); ++k) idx[k] = k;
+    std::stable_sort(idx.begin(), idx.end(),
+                     [&](size_t a, size_t b) { return work[a] > work[b]; });
+    for (size_t k : idx) {
       ApplyItem it = stItems[s][k];
       it.contrib0 = (int64_t)prog.contribs.size();
       for (auto const &c : stContribs[s][k]) prog.contribs.push_back(c);

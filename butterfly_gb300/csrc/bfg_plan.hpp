@@ -62,6 +62,7 @@ struct Block {
   int64_t s0 = 0, s1 = 0, t0 = 0, t1 = 0;
   Circle corig, ceq, cchk;
   int64_t arenaOff = 0;         // complex entries, column-major m x n
+  double k = 0;                 // wavenumber of the block's problem
 };
 
 struct Factor {
@@ -98,6 +99,13 @@ struct Plan {
   std::vector<Product> products;
   std::vector<PNode> pnodes;
   int32_t root = -1;
+  // one HODBF root per problem with the tree-order row / column offsets of
+  // that problem (a single problem has one root at (0, 0))
+  struct Root {
+    int32_t pnode;
+    int64_t rowBase, colBase;
+  };
+  std::vector<Root> roots;
   int64_t arenaEntries = 0;
   // block indices in plan order (the order of the plan text); the arena
   // stores the blocks back to back in this order
@@ -105,6 +113,14 @@ struct Plan {
 
   std::string text() const;     // the plan grammar of the oracle driver
 };
+
+// Independent problems in one plan: problem p has sources
+// srcXy[2*srcOff[p] .. 2*srcOff[p+1]) and targets likewise, wavenumber k[p];
+// the merged plan's rows and columns are the problems' tree orders back to
+// back, and its perms index the concatenated point arrays.
+void makePlanBatched(Plan &plan, PlanParams const &params, double const *k,
+                     double const *srcXy, int64_t const *srcOff, double const *tgtXy,
+                     int64_t const *tgtOff, int64_t numProblems);
 
 // Builds trees and the plan; throws std::runtime_error on geometry the
 // reference cannot factor.
@@ -162,6 +178,7 @@ struct FillDesc {
   int64_t arenaOff;
   int64_t s0, t0;               // tree-order point offsets
   double corig[3], ceq[3], cchk[3];
+  double k;                     // wavenumber
 };
 
 }  // namespace bfg

@@ -117,6 +117,21 @@ bfgStatus bfgFacHelm2MakeMultilevel(bfgContext ctx, bfgHelm2 const *helm,
                                     int64_t numSrc, double const *tgtXy,
                                     double const *tgtNormals, int64_t numTgt,
                                     bfgFacOptions const *opts, bfgFac *fac);
+/* Many independent problems of uneven size in one factorization: problem p
+ * has sources srcXy[2*srcOffsets[p] .. 2*srcOffsets[p+1]) (normals alike),
+ * targets alike, wavenumber k[p], and helm's layer potential and alpha/beta.
+ * Every kernel launch covers the blocks of all problems.  The result is the
+ * block-diagonal operator diag(A_0, ..., A_{P-1}): its rows and columns are
+ * the problems' tree orders back to back (bfgFacGetPerms maps them into the
+ * concatenated point arrays), so one apply serves every problem.  No
+ * counterpart call in the reference; each A_p equals
+ * bfFacHelm2MakeMultilevel of problem p (fac_helm2.c:943-1002). */
+bfgStatus bfgFacHelm2MakeBatched(bfgContext ctx, bfgHelm2 const *helm, double const *k,
+                                 int64_t numProblems, double const *srcXy,
+                                 double const *srcNormals, int64_t const *srcOffsets,
+                                 double const *tgtXy, double const *tgtNormals,
+                                 int64_t const *tgtOffsets, bfgFacOptions const *opts,
+                                 bfgFac *fac);
 /* bfMatDelete on the factorization (mat.h:57). */
 bfgStatus bfgFacDestroy(bfgFac fac);
 /* bfMatGetNumRows / bfMatGetNumCols (mat.c). */
