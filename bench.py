@@ -290,7 +290,12 @@ def main():
     stream.synchronize()
     yd = yd.cpu().numpy()
 
-    precs = {"fp64": (X64, Y64), "fp32": (X32, Y32)}
+    with torch.cuda.stream(stream):
+        Y16 = torch.empty((n, R), dtype=torch.complex64, device="cuda")
+    stream.synchronize()
+    # bf16x3 / bf16x2: tensor-core products of split-BF16 planes, complex64 vectors
+    precs = {"fp64": (X64, Y64), "fp32": (X32, Y32), "bf16x3": (X32, Y16),
+             "bf16x2": (X32, Y16)}
     errs = {}
     for p, (X, Y) in precs.items():
         fac.apply_device(X.data_ptr(), R, R, Y.data_ptr(), R, p)
@@ -333,7 +338,7 @@ def main():
     per = np.mean(np.array(per, dtype=np.float64), axis=0)
     info = fac.launch_info()
     dom = int(np.argmax(per))
-    sA = 16 if head == "fp64" else 8
+    sA = {"fp64": 16, "fp32": 8, "bf16x3": 12, "bf16x2": 8}[head]
     sv = 16 if head == "fp64" else 8
     alg_bytes = float(info[dom, 0] * sA + R * sv * (info[dom, 1] + info[dom, 2]))
     launch_share = [float(v) for v in per / per.sum()]
@@ -392,7 +397,9 @@ def main():
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_ms[head] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "complex64" if head == "fp32" else "complex128",
+            "dtype": {"fp64": "complex128", "fp32": "complex64",
+                      "bf16x3": "bf16x3 split (complex64 vectors)",
+                      "bf16x2": "bf16x2 split (complex64 vectors)"}[head],
             "data": "synthetic", "config": config_json(args.config, cfg, R),
             "precision": head, "rel_err": errs[head], "rel_err_all": errs,
             "rhs_per_s_all": rhs_s, "err_bound": ERR_BOUND,

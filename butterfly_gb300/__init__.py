@@ -24,7 +24,7 @@ LIB_PATH = os.path.join(_PKG, "libbfg.so")
 
 BFG_OK = 0
 APPLY_ORIGINAL_ORDER = 1
-PRECISIONS = {"fp64": 0, "fp32": 1}
+PRECISIONS = {"fp64": 0, "fp32": 1, "bf16x2": 2, "bf16x3": 3}
 STATUS_NAMES = {0: "OK", 1: "INVALID_ARGUMENTS", 2: "RUNTIME", 3: "NOT_IMPLEMENTED",
                 4: "MEMORY", 5: "OUT_OF_RANGE", 8: "INCOMPATIBLE_SHAPES", 32: "CUDA",
                 33: "TIMEOUT", 34: "NUMERICAL"}

@@ -82,6 +82,15 @@ struct bfgFac_s {
   DevBuf ws, xbuf;
   DevBuf hx128, hy128, hx64, hy64;  // staging of the host-operand apply
   std::vector<int64_t> stageItem0;
+  // split-BF16 tensor-core apply, per plane count (index terms - 2): the
+  // chunk schedule of the 128-row program and the bf16 planes of the factors
+  struct Tc {
+    bool ready = false;
+    int32_t ctas = 0;
+    size_t stages = 0;
+    DevBuf chunks, ctaChunk0, arena;
+  } tc[2];
+  DevBuf tcStatus;                  // kStatusTcTimeout from the tensor-core kernel
 };
 
 namespace {
@@ -413,6 +422,106 @@ void ensureArena32(bfgFac f) {
   f->arena32Ready = true;
 }
 
+bool isTcPrecision(bfgPrecision p) {
+  return p == BFG_PRECISION_BF16X2 || p == BFG_PRECISION_BF16X3;
+}
+
+// Builds the tensor-core program, schedule and bf16 planes for `terms`
+// planes (once per factorization and plane count).
+void ensureTc(bfgFac f, int terms) {
+  bfgFac_s::Tc &tc = f->tc[terms - 2];
+  if (tc.ready) return;
+  cudaStream_t s = f->ctx->stream;
+  int32_t perSm = 0;
+  ck(bfg::tcPrepare(terms, &perSm), "tensor-core apply");
+  int sms = 0;
+  ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, f->ctx->device), "device");
+  if (perSm < 1) throw BfgError{BFG_ERROR_RUNTIME, "tensor-core apply: kernel does not fit an SM"};
+  bfg::ApplyProgram p128;
+  bfg::makeApplyProgram(f->plan, p128, bfg::kTcRows);
+  if (p128.wsRows != f->prog.wsRows || p128.stageItem0.size() != f->stageItem0.size())
+    throw BfgError{BFG_ERROR_RUNTIME, "tensor-core apply: program mismatch"};
+  bfg::TcSchedule sc;
+  bfg::makeTcSchedule(p128, terms, perSm * sms, sc);
+  upload(tc.chunks, sc.chunks, s, "tensor-core schedule");
+  upload(tc.ctaChunk0, sc.ctaChunk0, s, "tensor-core schedule");
+  DevBuf fills;
+  upload(fills, sc.fills, s, "tensor-core schedule");
+  ck(tc.arena.ensure((size_t)std::max<int64_t>(16, sc.arenaBytes)), "tensor-core factors");
+  ck(bfg::launchTcFill(terms, fills.as<bfg::TcFill>(), (int64_t)sc.fills.size(),
+                       f->arena64.as<double2>(), tc.arena.as<uint8_t>(), s),
+     "tensor-core factors");
+  if (!f->tcStatus.p) {
+    ck(f->tcStatus.ensure(sizeof(int32_t)), "status");
+    ck(cudaMemsetAsync(f->tcStatus.p, 0, sizeof(int32_t), s), "status");
+  }
+  ck(cudaStreamSynchronize(s), "tensor-core factors");
+  tc.ctas = sc.ctas;
+  tc.stages = p128.stageItem0.size() - 1;
+  tc.ready = true;
+}
+
+// the tensor-core kernel's status word (synchronises); a bounded wait that
+// ran out is reported as BFG_ERROR_TIMEOUT
+void checkTcStatus(bfgFac f) {
+  if (!f->tcStatus.p) return;
+  int32_t st = 0;
+  ck(cudaMemcpyAsync(&st, f->tcStatus.p, sizeof st, cudaMemcpyDeviceToHost, f->ctx->stream),
+     "status");
+  ck(cudaStreamSynchronize(f->ctx->stream), "status");
+  if (st & bfg::kStatusTcTimeout) {
+    cudaMemsetAsync(f->tcStatus.p, 0, sizeof(int32_t), f->ctx->stream);
+    throw BfgError{BFG_ERROR_TIMEOUT, "tensor-core apply: a copy or MMA wait timed out"};
+  }
+}
+
+void runApplyTc(bfgFac f, int terms, float2 const *X, int64_t ldx, int64_t R, float2 *Y,
+                int64_t ldy, uint32_t flags, std::vector<cudaEvent_t> *events) {
+  cudaStream_t s = f->ctx->stream;
+  bfg::ApplyProgram const &p = f->prog;
+  bfgFac_s::Tc &tc = f->tc[terms - 2];
+  ck(f->ws.ensure((size_t)std::max<int64_t>(1, p.wsRows) * R * sizeof(float2)), "workspace");
+  float2 *W = f->ws.as<float2>();
+  float2 const *Xt = X;
+  int64_t ldxt = ldx;
+  size_t ev = 0;
+  auto mark = [&]() {
+    if (events) ck(cudaEventRecord((*events)[ev++], s), "event");
+  };
+  mark();
+  if (flags & BFG_APPLY_ORIGINAL_ORDER) {
+    ck(f->xbuf.ensure((size_t)p.numCols * R * sizeof(float2)), "gather buffer");
+    ck(bfg::launchGatherRows<float2>(X, ldx, f->srcPerm.as<int64_t>(), p.numCols, R,
+                                     f->xbuf.as<float2>(), s),
+       "gather");
+    Xt = f->xbuf.as<float2>();
+    ldxt = R;
+    mark();
+  }
+  for (size_t st = 0; st < tc.stages; ++st) {
+    ck(bfg::launchApplyTc(terms, tc.chunks.as<bfg::TcChunk>(),
+                          tc.ctaChunk0.as<int64_t>() + st * (size_t)(tc.ctas + 1), tc.ctas,
+                          tc.arena.as<uint8_t>(), Xt, ldxt, W, R, f->tcStatus.as<int32_t>(), s),
+       "tensor-core apply stage");
+    mark();
+  }
+  ck(bfg::launchApplyReduce<float2>(f->rowSeg.as<int32_t>(), f->segStart.as<int64_t>(),
+                                    f->segContrib0.as<int64_t>(), f->segBase.as<int64_t>(), W, R,
+                                    Y, ldy, p.numRows,
+                                    (flags & BFG_APPLY_ORIGINAL_ORDER) ? f->tgtPerm.as<int64_t>()
+                                                                      : nullptr,
+                                    s),
+     "apply reduce");
+  mark();
+}
+
+// one-time preparation of a precision's copy of the factors
+void preparePrecision(bfgFac f, bfgPrecision prec) {
+  if (prec == BFG_PRECISION_FP32) ensureArena32(f);
+  if (prec == BFG_PRECISION_BF16X2) ensureTc(f, 2);
+  if (prec == BFG_PRECISION_BF16X3) ensureTc(f, 3);
+}
+
 bfgStatus applyDispatch(bfgFac f, bfgPrecision prec, void const *X, int64_t ldx, int64_t R,
                         void *Y, int64_t ldy, uint32_t flags, std::vector<cudaEvent_t> *ev) {
   if (!X || !Y || R < 1 || ldx < R || ldy < R)
@@ -426,6 +535,11 @@ bfgStatus applyDispatch(bfgFac f, bfgPrecision prec, void const *X, int64_t ldx,
     ensureArena32(f);
     runApply<float2>(f, f->arena32.as<float2>(), static_cast<float2 const *>(X), ldx, R,
                      static_cast<float2 *>(Y), ldy, flags, ev);
+  } else if (isTcPrecision(prec)) {
+    int const terms = prec == BFG_PRECISION_BF16X3 ? 3 : 2;
+    ensureTc(f, terms);
+    runApplyTc(f, terms, static_cast<float2 const *>(X), ldx, R, static_cast<float2 *>(Y), ldy,
+               flags, ev);
   } else {
     return fail(f->ctx, BFG_ERROR_NOT_IMPLEMENTED, "apply: unknown precision");
   }
@@ -760,7 +874,7 @@ bfgStatus bfgFacApplyTimed(bfgFac f, bfgPrecision prec, void const *X, int64_t l
     size_t const n = numApplyLaunches(f, flags);
     *numLaunches = (int32_t)n;
     if (!ms || cap < (int32_t)n) return fail(f->ctx, BFG_ERROR_OUT_OF_RANGE, "timed apply: buffer too small");
-    if (prec == BFG_PRECISION_FP32) ensureArena32(f);
+    preparePrecision(f, prec);
     std::vector<cudaEvent_t> ev(n + 1);
     for (auto &e : ev) ck(cudaEventCreate(&e), "event");
     bfgStatus st = applyDispatch(f, prec, X, ldx, R, Y, ldy, flags, &ev);
@@ -769,6 +883,7 @@ bfgStatus bfgFacApplyTimed(bfgFac f, bfgPrecision prec, void const *X, int64_t l
       for (size_t i = 0; i < n; ++i) cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);
     }
     for (auto &e : ev) cudaEventDestroy(e);
+    if (st == BFG_OK && isTcPrecision(prec)) checkTcStatus(f);
     return st;
   });
 }
@@ -816,7 +931,7 @@ bfgStatus bfgFacApplyHost(bfgFac f, bfgPrecision prec, double const *X, int64_t 
     if (prec == BFG_PRECISION_FP64) {
       bfgStatus st = applyDispatch(f, prec, f->hx128.p, R, R, f->hy128.p, R, flags, nullptr);
       if (st != BFG_OK) return st;
-    } else if (prec == BFG_PRECISION_FP32) {
+    } else if (prec == BFG_PRECISION_FP32 || isTcPrecision(prec)) {
       ck(f->hx64.ensure((size_t)nc * R * 8), "apply buffers");
       ck(f->hy64.ensure((size_t)nr * R * 8), "apply buffers");
       ck(bfg::launchC128ToC64(f->hx128.as<double2>(), R, nc, R, f->hx64.as<float2>(), R, s),
@@ -832,6 +947,7 @@ bfgStatus bfgFacApplyHost(bfgFac f, bfgPrecision prec, double const *X, int64_t 
                          (size_t)nr, cudaMemcpyDeviceToHost, s),
        "copy Y");
     ck(cudaStreamSynchronize(s), "apply");
+    if (isTcPrecision(prec)) checkTcStatus(f);
     return BFG_OK;
   });
 }

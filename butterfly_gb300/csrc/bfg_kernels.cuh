@@ -97,6 +97,19 @@ cudaError_t launchApplyReduce(int32_t const *rowSeg, int64_t const *segStart,
                               int64_t nRows, int64_t const *outPerm,
                               cudaStream_t stream);
 
+// Split-BF16 tensor-core apply (terms = 2 or 3 bf16 planes).
+int32_t tcSmemBytes(int32_t terms);
+// sets the kernel's shared-memory limit; returns resident CTAs per SM
+cudaError_t tcPrepare(int32_t terms, int32_t *ctasPerSm);
+cudaError_t launchTcFill(int32_t terms, TcFill const *fills, int64_t nFills,
+                         double2 const *arena64, uint8_t *tarena, cudaStream_t stream);
+// one stage: `ctas` persistent CTAs (x) times RHS tiles of 16 (y); CTA c runs
+// chunks [ctaChunk0[c], ctaChunk0[c+1]); status bit 4 = a bounded wait expired
+cudaError_t launchApplyTc(int32_t terms, TcChunk const *chunks, int64_t const *ctaChunk0,
+                          int32_t ctas, uint8_t const *tarena, float2 const *X, int64_t ldx,
+                          float2 *W, int64_t R, int32_t *status, cudaStream_t stream);
+enum : int32_t { kStatusTcTimeout = 4 };
+
 // X_tree[i] = X[perm[i]] (row gather, R columns)
 template <typename T2>
 cudaError_t launchGatherRows(T2 const *X, int64_t ldx, int64_t const *perm,

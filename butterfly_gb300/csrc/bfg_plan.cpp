@@ -623,7 +623,7 @@ std::string Plan::text() const {
 // ---------------------------------------------------------------------------
 // Apply program
 // ---------------------------------------------------------------------------
-void makeApplyProgram(Plan const &plan, ApplyProgram &prog) {
+void makeApplyProgram(Plan const &plan, ApplyProgram &prog, int itemRows) {
   prog = ApplyProgram();
   prog.numRows = (int64_t)plan.tgt.perm.size();
   prog.numCols = (int64_t)plan.src.perm.size();
@@ -649,10 +649,10 @@ void makeApplyProgram(Plan const &plan, ApplyProgram &prog) {
                           std::vector<std::pair<Block const *, int64_t>> const &blks,
                           int inIsX) {
     // blks: (block, first input row); all share the block row
-    for (int64_t r0 = 0; r0 < rows; r0 += kItemRows) {
+    for (int64_t r0 = 0; r0 < rows; r0 += itemRows) {
       ApplyItem it{};
       it.outRow = outBase + r0;
-      it.rows = (int32_t)std::min<int64_t>(kItemRows, rows - r0);
+      it.rows = (int32_t)std::min<int64_t>(itemRows, rows - r0);
       std::vector<ApplyContrib> cs;
       for (auto const &bp : blks) {
         ApplyContrib c{};
@@ -792,6 +792,80 @@ void makeApplyProgram(Plan const &plan, ApplyProgram &prog) {
     for (int64_t c : segC[s]) prog.segBase.push_back(c);
     prog.segContrib0.push_back((int64_t)prog.segBase.size());
   }
+}
+
+void makeTcSchedule(ApplyProgram const &prog, int terms, int ctas, TcSchedule &sc) {
+  sc = TcSchedule();
+  sc.ctas = ctas;
+  size_t const nStages = prog.stageItem0.empty() ? 0 : prog.stageItem0.size() - 1;
+  int64_t arena = 0;
+  for (size_t s = 0; s < nStages; ++s) {
+    int64_t const a = prog.stageItem0[s], b = prog.stageItem0[s + 1];
+    // chunks of every item of the stage, in item order
+    std::vector<std::vector<TcChunk>> itemChunks((size_t)(b - a));
+    std::vector<int64_t> cost((size_t)(b - a), 0);
+    for (int64_t i = a; i < b; ++i) {
+      ApplyItem const &it = prog.items[(size_t)i];
+      int32_t const mg = (it.rows + 7) / 8;
+      auto &ch = itemChunks[(size_t)(i - a)];
+      for (int32_t c = 0; c < it.nContrib; ++c) {
+        ApplyContrib const &cb = prog.contribs[(size_t)(it.contrib0 + c)];
+        int32_t const width = 4 * tcMaxKGroups(mg);
+        for (int32_t cj = 0; cj < cb.n; cj += width) {
+          TcChunk k{};
+          k.nc = std::min(width, cb.n - cj);
+          k.kg = (k.nc + 3) / 4;
+          k.mg = mg;
+          k.rows = it.rows;
+          k.inRow = cb.inRow + cj;
+          k.inIsX = cb.inIsX;
+          k.outRow = it.outRow;
+          k.tileOff = arena;
+          TcFill f{};
+          f.srcOff = cb.aOff + (int64_t)cj * cb.lda;
+          f.tileOff = arena;
+          f.lda = cb.lda;
+          f.rows = it.rows;
+          f.nc = k.nc;
+          f.kg = k.kg;
+          f.mg = mg;
+          sc.fills.push_back(f);
+          arena += (int64_t)terms * k.kg * mg * 128;
+          ch.push_back(k);
+          // a chunk costs its tile bytes plus a fixed handshake
+          cost[(size_t)(i - a)] += (int64_t)k.kg * mg + 8;
+        }
+      }
+      // every block has at least one column, so every item has a chunk
+      if (ch.empty()) throw std::runtime_error("apply item without columns");
+      ch.front().flags |= kTcFirst;
+      ch.back().flags |= kTcLast;
+    }
+    // longest item first to the least-loaded CTA
+    std::vector<size_t> order((size_t)(b - a));
+    for (size_t k = 0; k < order.size(); ++k) order[k] = k;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t x, size_t y) { return cost[x] > cost[y]; });
+    std::vector<std::vector<size_t>> perCta((size_t)ctas);
+    std::vector<int64_t> load((size_t)ctas, 0);
+    for (size_t k : order) {
+      size_t best = 0;
+      for (size_t c = 1; c < (size_t)ctas; ++c)
+        if (load[c] < load[best]) best = c;
+      perCta[best].push_back(k);
+      load[best] += cost[k];
+    }
+    for (int c = 0; c < ctas; ++c) {
+      sc.ctaChunk0.push_back((int64_t)sc.chunks.size());
+      int64_t n0 = (int64_t)sc.chunks.size();
+      for (size_t k : perCta[(size_t)c])
+        for (TcChunk const &ch : itemChunks[k]) sc.chunks.push_back(ch);
+      sc.maxChunksPerCta =
+          std::max<int32_t>(sc.maxChunksPerCta, (int32_t)((int64_t)sc.chunks.size() - n0));
+    }
+    sc.ctaChunk0.push_back((int64_t)sc.chunks.size());
+  }
+  sc.arenaBytes = arena;
 }
 
 }  // namespace bfg

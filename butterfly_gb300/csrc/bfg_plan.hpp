@@ -170,7 +170,62 @@ struct ApplyProgram {
   int64_t sumRows = 0;
 };
 
-void makeApplyProgram(Plan const &plan, ApplyProgram &prog);
+// itemRows: rows per work item (32 for the CUDA-core kernels, 128 for the
+// tensor-core kernel, whose MMA tile is 128 rows high)
+void makeApplyProgram(Plan const &plan, ApplyProgram &prog, int itemRows = kItemRows);
+
+// ---------------------------------------------------------------------------
+// Tensor-core (split-BF16) apply: chunks of an item's contributions, each
+// stored as a pre-tiled bf16 A tile in the tensor arena.
+// ---------------------------------------------------------------------------
+constexpr int kTcRows = 128;          // MMA M: rows per item
+constexpr int kTcChunkCols = 64;      // most complex columns per chunk (8 MMA k-steps)
+// k-groups (4 complex columns) per chunk for an item of mg row groups: an A
+// plane holds at most 64 cores (8 KB), the count is even (whole k-steps)
+inline int32_t tcMaxKGroups(int32_t mg) {
+  int32_t k = 64 / (mg < 1 ? 1 : mg);
+  if (k > kTcChunkCols / 4) k = kTcChunkCols / 4;
+  return k & ~1;
+}
+
+// One chunk of the chunk stream of a persistent CTA.  The A tile of a chunk
+// holds `terms` bf16 planes back to back, each kg x mg core matrices of
+// 8 rows x 16 bytes, k-group-major: core (g, h) at (g * mg + h) * 128 bytes.
+struct TcChunk {
+  int64_t tileOff;              // bytes: plane 0 of the A tile
+  int64_t inRow;                // first input row (X or workspace)
+  int64_t outRow;               // first output row of the chunk's item
+  int32_t nc;                   // complex columns (<= 4 tcMaxKGroups(mg))
+  int32_t kg;                   // k-groups (4 complex columns each) = ceil(nc / 4)
+  int32_t mg;                   // row groups (8 rows each) = ceil(rows / 8)
+  int32_t rows;                 // rows of the item (<= kTcRows)
+  int32_t inIsX;
+  int32_t flags;                // bit 0: first chunk of its item, bit 1: last
+};
+constexpr int32_t kTcFirst = 1, kTcLast = 2;
+
+// Conversion of one chunk of the FP64 arena into its A tile.
+struct TcFill {
+  int64_t srcOff;               // FP64 arena entry of (item row 0, chunk column 0)
+  int64_t tileOff;
+  int32_t lda, rows, nc, kg, mg, pad;
+};
+
+struct TcSchedule {
+  int32_t ctas = 0;                       // persistent CTAs per RHS tile
+  // per stage s: chunk range of CTA c is ctaChunk0[s * (ctas + 1) + c] ..
+  // ctaChunk0[s * (ctas + 1) + c + 1]
+  std::vector<int64_t> ctaChunk0;
+  std::vector<TcChunk> chunks;
+  std::vector<TcFill> fills;
+  int64_t arenaBytes = 0;                 // bytes of all tiles (every plane)
+  int32_t maxChunksPerCta = 0;
+};
+
+// Splits the 128-row program's items into chunks and deals each stage's items
+// to `ctas` CTAs, longest first to the least-loaded CTA.  Tile offsets are in
+// bytes for `terms` planes per tile.
+void makeTcSchedule(ApplyProgram const &prog128, int terms, int ctas, TcSchedule &sched);
 
 // Fill descriptors for the kernel-evaluation and re-expansion kernels.
 struct FillDesc {

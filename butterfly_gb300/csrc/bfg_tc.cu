@@ -1,0 +1,569 @@
+// Split-BF16 apply of butterfly factors on the 5th-generation tensor cores
+// (tcgen05.mma, accumulator in tensor memory, operands staged by the bulk
+// copy engine).  This is the GB300 form of the reference's per-block
+// cblas_zgemm (mat_dense_complex.c:1705-1766) for the FP32-vector precisions:
+// the stored blocks are split into TERMS bf16 planes (hi, lo[, lo2]) once,
+// each right-hand side is split the same way as it is staged, and the complex
+// product is formed from real bf16 MMAs with FP32 accumulation.
+//
+// Complex -> real mapping (one MMA per pair of planes and k-step):
+//   A_real (128 rows x 2n) : row m = Re a_m0, Im a_m0, Re a_m1, Im a_m1, ...
+//   B      (2n x 32)       : rows 2j, 2j+1 of column q   = ( Re x_jq, -Im x_jq)
+//                            rows 2j, 2j+1 of column 16+q = ( Im x_jq,  Re x_jq)
+//   D = A_real B           : column q = Re y_q, column 16+q = Im y_q
+// so the stored block needs no duplication and the output lands in TMEM as
+// one row per lane.
+//
+// Products kept: TERMS = 2 -> hh + hl + lh (bf16x2, ~16 significant bits);
+// TERMS = 3 -> additionally h l2 + l l + l2 h (bf16x3, ~24 bits, FP32-like).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "bfg_kernels.cuh"
+
+namespace bfg {
+namespace {
+
+constexpr int kTcStages = 3;
+constexpr int kTcRhs = 16;                 // RHS per CTA
+constexpr int kTcN = 2 * kTcRhs;           // MMA N: real and imaginary columns
+constexpr int kAPlaneBytes = 64 * 128;     // at most 64 core matrices per plane
+constexpr int kBPlaneBytes = (kTcChunkCols / 4) * (kTcN / 8) * 128;      // 8 KB
+constexpr int kBuilders = 256;             // warps 0-7: B planes and epilogue
+constexpr int kProducerWarp = kBuilders / 32, kMmaWarp = kProducerWarp + 1;
+constexpr int kTcThreads = kBuilders + 64; // then one warp of bulk copies, one of MMAs
+constexpr uint64_t kWaitLimitNs = 1000000000ull;                          // 1 s
+
+constexpr int kXStageBytes = kTcChunkCols * kTcRhs * 8;                   // 8 KB
+
+template <int TERMS>
+struct TcLayout {
+  // B planes interleaved by k-group: k-group g holds plane 0's four n-groups,
+  // then plane 1's, ... so that planes u .. TERMS-1 form one N = 32 (TERMS-u)
+  // operand; bytes of one k-group:
+  static constexpr int kBKGroupBytes = TERMS * (kTcN / 8) * 128;
+  static constexpr int aBytes = TERMS * kAPlaneBytes;
+  static constexpr int bBytes = TERMS * kBPlaneBytes;
+  // A planes, B planes, then the chunk's FP32 right-hand sides
+  static constexpr int stageBytes = aBytes + bBytes + kXStageBytes;
+  // an A descriptor spans 16 row groups and the last k-step reads up to 2 KB
+  // past a short tile (rows whose outputs are discarded): 2 KB of slack
+  // follow the last stage
+  static constexpr int barOff = kTcStages * stageBytes + 2048;
+  // fullA[S], fullB[S], empty[S], accFull[2], accEmpty[2], TMEM slot, abort
+  static constexpr int smemBytes = barOff + 8 * (3 * kTcStages + 4) + 16;
+};
+
+// instruction descriptor: D f32, A and B bf16, both K-major, M = 128, N = n
+__host__ __device__ constexpr uint32_t idescN(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(kTcRows >> 4) << 24);
+}
+
+__device__ __forceinline__ uint32_t smemAddr(void const *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// shared-memory matrix descriptor, no swizzle: core matrices of 8 rows x 16 B;
+// lbo = bytes between K-adjacent cores, sbo = bytes between M/N-adjacent cores
+__device__ __forceinline__ uint64_t smemDesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ void mbarInit(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fenceMbarInit() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbarExpectTx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbarTryWait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ uint64_t globalTimerNs() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// waits for the phase with the given parity; false after kWaitLimitNs or as
+// soon as another role of the CTA has given up (*abort set)
+__device__ bool mbarWait(uint32_t bar, uint32_t parity, int volatile *abort) {
+  if (mbarTryWait(bar, parity)) return true;
+  uint64_t const t0 = globalTimerNs();
+  for (;;) {
+    if (mbarTryWait(bar, parity)) return true;
+    if (*abort || globalTimerNs() - t0 > kWaitLimitNs) return false;
+  }
+}
+// the same wait without the early exit (draining work in flight)
+__device__ void mbarDrain(uint32_t bar, uint32_t parity) {
+  uint64_t const t0 = globalTimerNs();
+  while (!mbarTryWait(bar, parity))
+    if (globalTimerNs() - t0 > kWaitLimitNs) return;
+}
+__device__ __forceinline__ void cpAsync8(uint32_t dst, float2 const *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpAsyncCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpAsyncWait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void mbarArrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void bulkG2S(uint32_t dst, void const *src, uint32_t bytes,
+                                        uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      ::"r"(dst), "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void fenceProxyAsync() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// two accumulator buffers of up to 96 FP32 columns, 128 apart
+__device__ __forceinline__ void tmemAlloc256(uint32_t slot) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(slot)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmemDealloc256(uint32_t taddr) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(taddr) : "memory");
+}
+__device__ __forceinline__ void tcFenceBefore() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tcFenceAfter() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tcMma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                      uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+      ::"r"(d), "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void tcCommit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      : "memory");
+}
+// v = t[0] + t[1] + ... with each t[i] the bf16 rounding of what is left
+template <int TERMS>
+__device__ __forceinline__ void splitD(double v, __nv_bfloat16 (&t)[TERMS]) {
+  double r = v;
+#pragma unroll
+  for (int i = 0; i < TERMS; ++i) {
+    t[i] = __double2bfloat16(r);
+    r -= (double)__bfloat162float(t[i]);
+  }
+}
+// (lo, hi) rounded to a bf16 pair, lo in the low half
+__device__ __forceinline__ uint32_t cvtPack(float lo, float hi) {
+  uint32_t r;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+  return r;
+}
+// (re, im) = sum over t of the bf16 pairs p[t], each the rounding of what is left
+template <int TERMS>
+__device__ __forceinline__ void splitPair(float re, float im, uint32_t (&p)[TERMS]) {
+#pragma unroll
+  for (int t = 0; t < TERMS; ++t) {
+    p[t] = cvtPack(re, im);
+    re -= __uint_as_float(p[t] << 16);
+    im -= __uint_as_float(p[t] & 0xFFFF0000u);
+  }
+}
+// 8 consecutive FP32 columns of this thread's TMEM lane (no wait)
+__device__ __forceinline__ void tmemLoad8(uint32_t taddr, float *v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                 "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr)
+               : "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmemWaitLoads() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+  return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+// FP64 arena -> bf16 planes of every chunk tile (one CTA per chunk, strided)
+template <int TERMS>
+__global__ void __launch_bounds__(256) tcFillKernel(TcFill const *__restrict__ fills,
+                                                    int64_t nFills,
+                                                    double2 const *__restrict__ arena,
+                                                    uint8_t *__restrict__ tarena) {
+  for (int64_t f = blockIdx.x; f < nFills; f += gridDim.x) {
+    TcFill const d = fills[f];
+    int const r8 = d.mg * 8, j4 = d.kg * 4;
+    int64_t const plane = (int64_t)d.kg * d.mg * 128;
+    for (int e = threadIdx.x; e < r8 * j4; e += blockDim.x) {
+      int const m = e % r8, j = e / r8;
+      double2 v = make_double2(0.0, 0.0);
+      if (m < d.rows && j < d.nc) v = arena[d.srcOff + (int64_t)j * d.lda + m];
+      __nv_bfloat16 re[TERMS], im[TERMS];
+      splitD<TERMS>(v.x, re);
+      splitD<TERMS>(v.y, im);
+      int64_t const off =
+          d.tileOff + ((int64_t)(j >> 2) * d.mg + (m >> 3)) * 128 + (m & 7) * 16 + (j & 3) * 4;
+#pragma unroll
+      for (int t = 0; t < TERMS; ++t)
+        *reinterpret_cast<uint32_t *>(tarena + off + t * plane) = pack2(re[t], im[t]);
+    }
+  }
+}
+
+// Persistent CTA over its chunk stream (one apply stage, one tile of 16 RHS),
+// warp-specialised around mbarriers:
+//   warp 4 (lane 0)  bulk-copies the A planes of chunk i into stage i % 3
+//                    once the MMAs of chunk i-3 are done (empty);
+//   warps 0-3        build the bf16 B planes of chunk i from registers loaded
+//                    one chunk ahead (fullB), then read chunk i-1's partial
+//                    sums from TMEM (accFull) into FP32 registers, release
+//                    the TMEM buffer (accEmpty) and store finished items;
+//   warp 5 (lane 0)  issues chunk i's MMAs into TMEM buffer i % 2 once its A
+//                    and B planes have landed and the buffer was read.
+// Each chunk starts its TMEM buffer from zero, so the tensor cores accumulate
+// at most 16 k-steps x products before the sum moves to FP32 registers.
+// Every wait is bounded (kWaitLimitNs) and gives up when another role has;
+// the CTA then waits (bounded) for the copies and MMAs it has in flight,
+// frees its TMEM and reports kStatusTcTimeout.
+template <int TERMS>
+__global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
+    TcChunk const *__restrict__ chunks, int64_t const *__restrict__ ctaChunk0,
+    uint8_t const *__restrict__ tarena, float2 const *__restrict__ X, int64_t ldx,
+    float2 *__restrict__ W, int64_t R, int32_t *status) {
+  using L = TcLayout<TERMS>;
+  constexpr int S = kTcStages;
+  constexpr int kBKGroupBytes = L::kBKGroupBytes;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  int const tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  int64_t const c0 = ctaChunk0[blockIdx.x];
+  int64_t const nCh = ctaChunk0[blockIdx.x + 1] - c0;
+  if (nCh <= 0) return;
+  int64_t const r0 = (int64_t)blockIdx.y * kTcRhs;
+  int const nr = (R - r0) < kTcRhs ? (int)(R - r0) : kTcRhs;
+  TcChunk const *ch = chunks + c0;
+
+  uint32_t const sbase = smemAddr(smem);
+  uint32_t const fullA = sbase + L::barOff, fullB = fullA + 8 * S, empty = fullB + 8 * S;
+  uint32_t const accFull = empty + 8 * S, accEmpty = accFull + 16;
+  uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(smem + L::barOff + 8 * (3 * S + 4));
+  int volatile *abortFlag = reinterpret_cast<int volatile *>(tmemSlot + 1);
+
+  if (tid == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbarInit(fullA + 8 * s, 1);
+      mbarInit(fullB + 8 * s, kBuilders / 32);
+      mbarInit(empty + 8 * s, 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbarInit(accFull + 8 * b, 1);
+      mbarInit(accEmpty + 8 * b, kBuilders / 32);
+    }
+    *abortFlag = 0;
+    fenceMbarInit();
+  }
+  if (warp == kMmaWarp) tmemAlloc256(smemAddr(tmemSlot));
+  tcFenceBefore();
+  __syncthreads();
+  tcFenceAfter();
+  uint32_t const tmem = *tmemSlot;
+
+  if (warp == kProducerWarp) {
+    // ---- bulk copies of the A planes ----
+    if (lane == 0) {
+      int64_t issued = 0;
+      // descriptors are read one chunk ahead, off the wait-issue path
+      int64_t off = ch[0].tileOff;
+      uint32_t plane = (uint32_t)ch[0].kg * ch[0].mg * 128;
+      for (int64_t i = 0; i < nCh; ++i) {
+        int const s = (int)(i % S);
+        int64_t offN = 0;
+        uint32_t planeN = 0;
+        if (i + 1 < nCh) {
+          offN = ch[i + 1].tileOff;
+          planeN = (uint32_t)ch[i + 1].kg * ch[i + 1].mg * 128;
+        }
+        if (i >= S && !mbarWait(empty + 8 * s, (uint32_t)((i / S - 1) & 1), abortFlag)) {
+          *abortFlag = 1;
+          break;
+        }
+        mbarExpectTx(fullA + 8 * s, plane * TERMS);
+#pragma unroll
+        for (int t = 0; t < TERMS; ++t)
+          bulkG2S(sbase + s * L::stageBytes + t * kAPlaneBytes, tarena + off + (int64_t)t * plane,
+                  plane, fullA + 8 * s);
+        issued = i + 1;
+        off = offN;
+        plane = planeN;
+      }
+      if (*abortFlag)   // copies still in flight land before the CTA exits
+        for (int64_t j = issued > S ? issued - S : 0; j < issued; ++j)
+          mbarDrain(fullA + 8 * (j % S), (uint32_t)((j / S) & 1));
+    }
+  } else if (warp == kMmaWarp) {
+    // ---- MMAs ----
+    if (lane == 0) {
+      int64_t last = -1;
+      int32_t kg = ch[0].kg, mg = ch[0].mg;
+      for (int64_t i = 0; i < nCh; ++i) {
+        int const s = (int)(i % S), b = (int)(i & 1);
+        uint32_t const ph = (uint32_t)((i / S) & 1);
+        int32_t kgN = 0, mgN = 0;
+        if (i + 1 < nCh) {
+          kgN = ch[i + 1].kg;
+          mgN = ch[i + 1].mg;
+        }
+        if (!mbarWait(fullA + 8 * s, ph, abortFlag) || !mbarWait(fullB + 8 * s, ph, abortFlag) ||
+            (i >= 2 && !mbarWait(accEmpty + 8 * b, (uint32_t)(((i >> 1) - 1) & 1), abortFlag))) {
+          *abortFlag = 1;
+          break;
+        }
+        tcFenceAfter();
+        uint32_t const aS = sbase + s * L::stageBytes, bS = aS + L::aBytes;
+        uint32_t const lboA = (uint32_t)mg * 128;
+        int const ksteps = (kg + 1) >> 1;
+        for (int st = 0; st < ksteps; ++st) {
+          // A plane t times the B planes 0 .. TERMS-1-t, side by side in N:
+          // D columns 32 u .. 32 u + 31 collect the products with B plane u
+          uint64_t const db = smemDesc(bS + 2 * st * kBKGroupBytes, kBKGroupBytes, 128);
+#pragma unroll
+          for (int t = 0; t < TERMS; ++t) {
+            uint64_t const da = smemDesc(aS + t * kAPlaneBytes + 2 * st * lboA, lboA, 128);
+            tcMma(tmem + 128 * b, da, db, idescN(kTcN * (TERMS - t)), (st | t) ? 1u : 0u);
+          }
+        }
+        tcCommit(empty + 8 * s);
+        tcCommit(accFull + 8 * b);
+        last = i;
+        kg = kgN;
+        mg = mgN;
+      }
+      if (*abortFlag && last >= 0)
+        mbarDrain(empty + 8 * (last % S), (uint32_t)((last / S) & 1));
+    }
+  } else {
+    // ---- B planes, partial sums, stores ----
+    // Half h = tid / 128 of the builders converts the k-steps st = h, h+2, ..
+    // Element (j, q) of a k-step's 8 columns x 16 RHS belongs to one thread
+    // of the half: j = 8 st + (lane & 3) + 4 (w & 1), q = (lane >> 2) + 8 (w >> 1)
+    // with w = its warp within the half, so a warp's B stores fall in 32
+    // distinct banks.  The thread that copies an element into the X stage is
+    // the one that converts it, so the cp.async groups need no barrier.
+    // For the partial sums half h takes RHS 8h .. 8h+7 of TMEM lane quarter w.
+    int const h = tid >> 7, w = warp & 3;
+    int const jOff = (lane & 3) + 4 * (w & 1), q = (lane >> 2) + 8 * (w >> 1);
+    float acc[kTcRhs];   // RHS 8h .. 8h+7: real parts, then imaginary parts
+#pragma unroll
+    for (int c = 0; c < kTcRhs; ++c) acc[c] = 0.f;
+    // chunk descriptors live in registers from one iteration before their
+    // first use (the cp.async of the chunk's inputs) to their last (its store)
+    struct Cd {
+      int64_t inRow, outRow;
+      int32_t nc, kg, mg, rows, inIsX, flags;
+    };
+    auto loadCd = [&](int64_t i) {
+      Cd d{};
+      if (i < nCh) {
+        TcChunk const &k = ch[i];
+        d = Cd{k.inRow, k.outRow, k.nc, k.kg, k.mg, k.rows, k.inIsX, k.flags};
+      }
+      return d;
+    };
+    auto issueX = [&](Cd const &d, int64_t i) {
+      int64_t const xld = d.inIsX ? ldx : R;
+      float2 const *src = (d.inIsX ? X : W) + d.inRow * xld + r0 + q;
+      uint32_t const xs = sbase + (int)(i % S) * L::stageBytes + L::aBytes + L::bBytes;
+      if (q < nr)
+        for (int j = 8 * h + jOff; j < d.nc; j += 16)
+          cpAsync8(xs + (uint32_t)(j * kTcRhs + q) * 8, src + (int64_t)j * xld);
+    };
+    // TMEM partial sums of chunk j into acc; stores the item after its last chunk
+    auto extract = [&](Cd const &d, int64_t j) -> bool {
+      int const b = (int)(j & 1);
+      if (!mbarWait(accFull + 8 * b, (uint32_t)((j >> 1) & 1), abortFlag)) return false;
+      tcFenceAfter();
+      uint32_t const tl = tmem + 128 * b + 8 * h + ((uint32_t)(w * 32) << 16);
+      float v[TERMS][kTcRhs];
+#pragma unroll
+      for (int u = 0; u < TERMS; ++u) {
+        tmemLoad8(tl + 32 * u, v[u]);                  // real parts
+        tmemLoad8(tl + 32 * u + kTcRhs, v[u] + 8);     // imaginary parts
+      }
+      tmemWaitLoads();
+#pragma unroll
+      for (int c = 0; c < kTcRhs; ++c) {
+        float t = v[TERMS - 1][c];   // products with the smallest B plane first
+#pragma unroll
+        for (int u = TERMS - 2; u >= 0; --u) t += v[u][c];
+        acc[c] += t;
+      }
+      tcFenceBefore();
+      __syncwarp();
+      if (lane == 0) mbarArrive(accEmpty + 8 * b);
+      if (d.flags & kTcLast) {
+        int const row = w * 32 + lane;
+        if (row < d.rows) {
+          float2 *out = W + (d.outRow + row) * R + r0 + 8 * h;
+#pragma unroll
+          for (int c = 0; c < 8; ++c)
+            if (8 * h + c < nr) out[c] = make_float2(acc[c], acc[8 + c]);
+        }
+#pragma unroll
+        for (int c = 0; c < kTcRhs; ++c) acc[c] = 0.f;
+      }
+      return true;
+    };
+    Cd dPrev{}, d0 = loadCd(0), d1 = loadCd(1), d2 = loadCd(2);
+    // inputs of chunks 0 and 1 in flight before the loop (two cp.async groups)
+    if (0 < nCh) issueX(d0, 0);
+    cpAsyncCommit();
+    if (1 < nCh) issueX(d1, 1);
+    cpAsyncCommit();
+    bool ok = true;
+    for (int64_t i = 0; i < nCh && ok; ++i) {
+      int const s = (int)(i % S);
+      Cd const d3 = loadCd(i + 3);   // used from the next iteration on
+      // inputs of chunk i+2 into its stage: that stage's X area last held
+      // chunk i-1, which this thread has converted
+      if (i + 2 < nCh) issueX(d2, i + 2);
+      cpAsyncCommit();
+      if (i >= S && !mbarWait(empty + 8 * s, (uint32_t)((i / S - 1) & 1), abortFlag)) {
+        ok = false;
+        break;
+      }
+      cpAsyncWait<2>();   // this thread's elements of chunk i have landed
+      uint8_t *stage = smem + s * L::stageBytes;
+      uint8_t *bsm = stage + L::aBytes;
+      float2 const *xs = reinterpret_cast<float2 const *>(stage + L::aBytes + L::bBytes);
+      int const ksteps = (d0.kg + 1) >> 1;
+      for (int st = h; st < ksteps; st += 2) {
+        int const j = 8 * st + jOff;
+        float2 const v = (j < d0.nc && q < nr) ? xs[j * kTcRhs + q] : make_float2(0.f, 0.f);
+        uint32_t pr[TERMS];
+        splitPair<TERMS>(v.x, v.y, pr);
+        int const kk = 2 * j;
+        uint32_t const offRe =
+            (kk >> 3) * kBKGroupBytes + (q >> 3) * 128 + (q & 7) * 16 + (kk & 7) * 2;
+        uint32_t const offIm = offRe + 2 * 128;   // column 16 + q: two core rows further
+#pragma unroll
+        for (int t = 0; t < TERMS; ++t) {
+          // rows 2j, 2j+1 of column q: (Re x, -Im x); of column 16+q: (Im x, Re x)
+          *reinterpret_cast<uint32_t *>(bsm + t * 512 + offRe) = pr[t] ^ 0x80000000u;
+          *reinterpret_cast<uint32_t *>(bsm + t * 512 + offIm) = __byte_perm(pr[t], 0, 0x1032);
+        }
+      }
+      // an odd k-group count leaves the second half of the last k-step unset
+      // in A: zero it (B is zero there, but stale shared memory may hold NaNs)
+      if (d0.kg & 1) {
+        uint32_t const padOff = (uint32_t)d0.kg * d0.mg * 128, padBytes = (uint32_t)d0.mg * 128;
+        for (uint32_t e = (uint32_t)tid * 16; e < padBytes; e += kBuilders * 16)
+#pragma unroll
+          for (int t = 0; t < TERMS; ++t)
+            *reinterpret_cast<uint4 *>(stage + t * kAPlaneBytes + padOff + e) =
+                make_uint4(0, 0, 0, 0);
+      }
+      fenceProxyAsync();
+      __syncwarp();
+      if (lane == 0) mbarArrive(fullB + 8 * s);
+      if (i >= 1 && !extract(dPrev, i - 1)) {
+        ok = false;
+        break;
+      }
+      dPrev = d0;
+      d0 = d1;
+      d1 = d2;
+      d2 = d3;
+    }
+    if (ok) ok = extract(dPrev, nCh - 1);
+    cpAsyncWait<0>();
+    if (!ok) *abortFlag = 1;
+  }
+
+  tcFenceBefore();
+  __syncthreads();
+  if (warp == kMmaWarp) {
+    __syncwarp();
+    tcFenceAfter();
+    tmemDealloc256(tmem);
+  }
+  if (tid == 0 && *abortFlag) atomicOr(status, kStatusTcTimeout);
+}
+
+}  // namespace
+
+int32_t tcSmemBytes(int32_t terms) {
+  return terms == 3 ? TcLayout<3>::smemBytes : TcLayout<2>::smemBytes;
+}
+
+cudaError_t tcPrepare(int32_t terms, int32_t *ctasPerSm) {
+  cudaError_t e;
+  int per = 0;
+  if (terms == 3) {
+    e = cudaFuncSetAttribute(applyTcKernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             TcLayout<3>::smemBytes);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, applyTcKernel<3>, kTcThreads,
+                                                      TcLayout<3>::smemBytes);
+  } else {
+    e = cudaFuncSetAttribute(applyTcKernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             TcLayout<2>::smemBytes);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, applyTcKernel<2>, kTcThreads,
+                                                      TcLayout<2>::smemBytes);
+  }
+  if (e != cudaSuccess) return e;
+  *ctasPerSm = per;
+  return cudaSuccess;
+}
+
+cudaError_t launchTcFill(int32_t terms, TcFill const *fills, int64_t nFills,
+                         double2 const *arena64, uint8_t *tarena, cudaStream_t stream) {
+  if (nFills == 0) return cudaSuccess;
+  unsigned const grid = (unsigned)(nFills < 152 * 64 ? nFills : 152 * 64);
+  if (terms == 3)
+    tcFillKernel<3><<<grid, 256, 0, stream>>>(fills, nFills, arena64, tarena);
+  else
+    tcFillKernel<2><<<grid, 256, 0, stream>>>(fills, nFills, arena64, tarena);
+  return cudaGetLastError();
+}
+
+cudaError_t launchApplyTc(int32_t terms, TcChunk const *chunks, int64_t const *ctaChunk0,
+                          int32_t ctas, uint8_t const *tarena, float2 const *X, int64_t ldx,
+                          float2 *W, int64_t R, int32_t *status, cudaStream_t stream) {
+  if (ctas == 0) return cudaSuccess;
+  dim3 grid((unsigned)ctas, (unsigned)((R + kTcRhs - 1) / kTcRhs));
+  if (terms == 3)
+    applyTcKernel<3><<<grid, kTcThreads, TcLayout<3>::smemBytes, stream>>>(chunks, ctaChunk0, tarena, X,
+                                                                     ldx, W, R, status);
+  else
+    applyTcKernel<2><<<grid, kTcThreads, TcLayout<2>::smemBytes, stream>>>(chunks, ctaChunk0, tarena, X,
+                                                                     ldx, W, R, status);
+  return cudaGetLastError();
+}
+
+}  // namespace bfg

@@ -47,7 +47,14 @@ typedef enum bfgLayerPotential {
 /* Arithmetic of an apply. */
 typedef enum bfgPrecision {
   BFG_PRECISION_FP64 = 0,   /* complex128 factors and vectors */
-  BFG_PRECISION_FP32 = 1    /* complex64 factors and vectors, FP32 accumulate */
+  BFG_PRECISION_FP32 = 1,   /* complex64 factors and vectors, FP32 accumulate */
+  /* Tensor-core products with complex64 vectors: factors and right-hand sides
+   * split into bf16 planes (hi + lo, or hi + lo + lo2), FP32 accumulate.
+   * BF16X2 stores 8 bytes per complex entry and keeps ~16 significant bits;
+   * BF16X3 stores 12 bytes and keeps ~24 bits (FP32-like).  The reference
+   * computes in complex128 only; these are GB300 additions. */
+  BFG_PRECISION_BF16X2 = 2,
+  BFG_PRECISION_BF16X3 = 3
 } bfgPrecision;
 
 typedef struct bfgContext_s *bfgContext;
@@ -153,7 +160,9 @@ bfgStatus bfgFacCopyBlocks(bfgFac fac, double *entries, int64_t capacityEntries,
 
 /* Y = A X -- bfMatMul (mat.c:183-185) with A the factorization.  X (numCols
  * x numRhs) and Y (numRows x numRhs) are DEVICE pointers: complex128 for
- * FP64, complex64 for FP32.  Rows are in tree order unless
+ * FP64, complex64 for FP32, BF16X2 and BF16X3.  The first apply in a
+ * precision other than FP64 builds that precision's copy of the factors
+ * (allocates and synchronises once).  Rows are in tree order unless
  * BFG_APPLY_ORIGINAL_ORDER is set.  Runs on the context's stream; returns
  * without synchronising. */
 bfgStatus bfgFacApply(bfgFac fac, bfgPrecision precision, void const *X, int64_t ldx,

@@ -1,0 +1,104 @@
+"""Split-BF16 tensor-core apply (tcgen05, precisions "bf16x2" and "bf16x3")
+against the FP64 apply, which matches the reference's own A_BF X to 1e-10,
+and against the reference's golden outputs.
+
+Tolerances (relative Frobenius error):
+  * bf16x3 -- 3e-6: three bf16 planes keep ~24 significant bits of every
+    factor entry and right-hand side (FP32 storage keeps 24), accumulated in
+    FP32 by the tensor cores;
+  * bf16x2 -- 2e-3: two planes keep ~16 bits.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_err
+from oracle import bf_oracle as O
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import butterfly_gb300 as B  # noqa: E402
+
+TOL = {"bf16x3": 3e-6, "bf16x2": 2e-3}
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return B.default_context(0)
+
+
+_facs = {}
+
+
+def golden_fac(name, ctx):
+    if name not in _facs:
+        g = load_golden(name)
+        fac = B.FacHelm2.make_multilevel(B.Helm2(float(g["k"])), B.Quadtree(g["src"]),
+                                         B.Quadtree(g["tgt"]), context=ctx)
+        _facs[name] = (g, fac)
+    return _facs[name]
+
+
+@pytest.mark.parametrize("prec", ["bf16x3", "bf16x2"])
+@pytest.mark.parametrize("R", [1, 5, 16, 40])
+def test_tensor_apply_close_to_fp64(ctx, prec, R):
+    g, fac = golden_fac("c1_circle_n4096_k64", ctx)
+    X = O.RefRng(11 + R).complex_randn(4096 * R).reshape(4096, R)
+    Xd = torch.from_numpy(X).cuda()
+    y64 = fac.apply(Xd).cpu().numpy()
+    y = fac.apply(Xd.to(torch.complex64), precision=prec).cpu().numpy().astype(np.complex128)
+    assert rel_err(y, y64) < TOL[prec]
+
+
+@pytest.mark.parametrize("name", ["star_n2048_k48", "ellipse_n16384_k128"])
+def test_tensor_apply_matches_reference_output(ctx, name):
+    """bf16x3 against the reference's own A_BF X (golden fixture)."""
+    g, fac = golden_fac(name, ctx)
+    y = fac.apply(torch.from_numpy(g["x"]).cuda().to(torch.complex64), precision="bf16x3")
+    y = y.cpu().numpy().astype(np.complex128)
+    assert rel_err(y, g["y_bf"].reshape(y.shape)) < TOL["bf16x3"]
+
+
+def test_tensor_apply_is_deterministic(ctx):
+    g, fac = golden_fac("star_n2048_k48", ctx)
+    X = torch.from_numpy(O.RefRng(3).complex_randn(2048 * 16).reshape(2048, 16)).cuda()
+    X = X.to(torch.complex64)
+    y1 = fac.apply(X, precision="bf16x3")
+    y2 = fac.apply(X, precision="bf16x3")
+    assert torch.equal(y1, y2)
+
+
+def test_tensor_apply_columns_are_independent(ctx):
+    """RHS tiles of 16 and the partial last tile give each column the result
+    of its own single-column apply."""
+    g, fac = golden_fac("star_n2048_k48", ctx)
+    X = O.RefRng(4).complex_randn(2048 * 21).reshape(2048, 21)
+    Xd = torch.from_numpy(X).cuda().to(torch.complex64)
+    y = fac.apply(Xd, precision="bf16x3").cpu().numpy()
+    for c in (0, 15, 16, 20):
+        yc = fac.apply(Xd[:, c:c + 1].contiguous(), precision="bf16x3").cpu().numpy()
+        assert np.array_equal(y[:, c:c + 1], yc)
+
+
+def test_tensor_apply_host_operands_and_original_order(ctx):
+    g, fac = golden_fac("star_n2048_k48", ctx)
+    sp, tp = fac.perms()
+    x_tree = g["x"]
+    x_orig = np.empty_like(x_tree)
+    x_orig[sp] = x_tree
+    y_tree = fac.apply(x_tree, precision="bf16x3")              # host complex128 path
+    y_orig = fac.apply(x_orig, precision="bf16x3", original_order=True)
+    assert rel_err(y_orig[tp], y_tree) < 1e-12
+    assert rel_err(y_tree, g["y_bf"].reshape(y_tree.shape)) < TOL["bf16x3"]
+
+
+def test_tensor_apply_timed_launch_count(ctx):
+    g, fac = golden_fac("star_n2048_k48", ctx)
+    X = torch.zeros((2048, 16), dtype=torch.complex64, device="cuda")
+    Y = torch.empty_like(X)
+    torch.cuda.synchronize()
+    ms = fac.apply_timed(X.data_ptr(), 16, 16, Y.data_ptr(), 16, "bf16x3")
+    assert len(ms) == len(fac.launch_info())
+    assert torch.count_nonzero(Y).item() == 0
