@@ -31,9 +31,10 @@ constexpr int kTcRhs = 16;                 // RHS per CTA
 constexpr int kTcN = 2 * kTcRhs;           // MMA N: real and imaginary columns
 constexpr int kAPlaneBytes = 64 * 128;     // at most 64 core matrices per plane
 constexpr int kBPlaneBytes = (kTcChunkCols / 4) * (kTcN / 8) * 128;      // 8 KB
-constexpr int kBuilders = 256;             // warps 0-7: B planes and epilogue
-constexpr int kProducerWarp = kBuilders / 32, kMmaWarp = kProducerWarp + 1;
-constexpr int kTcThreads = kBuilders + 64; // then one warp of bulk copies, one of MMAs
+constexpr int kBuilders = 128;             // warps 0-3: B planes
+constexpr int kExtractors = 128;           // warps 4-7: TMEM partial sums and stores
+constexpr int kProducerWarp = (kBuilders + kExtractors) / 32, kMmaWarp = kProducerWarp + 1;
+constexpr int kTcThreads = kBuilders + kExtractors + 64;   // + bulk-copy warp + MMA warp
 constexpr uint64_t kWaitLimitNs = 1000000000ull;                          // 1 s
 
 constexpr int kXStageBytes = kTcChunkCols * kTcRhs * 8;                   // 8 KB
@@ -56,7 +57,10 @@ struct TcLayout {
   static constexpr int smemBytes = barOff + 8 * (3 * kTcStages + 4) + 16;
 };
 
-// instruction descriptor: D f32, A and B bf16, both K-major, M = 128, N = n
+// instruction descriptor: D f32, A and B bf16, both K-major, M = 128, N = n.
+// D row r lands in TMEM lane r.  (An MMA costs at least ~44 cycles whatever
+// its size and M = 64 runs at half the rate of M = 128, so every chunk uses
+// M = 128 and as wide an N as the planes allow.)
 __host__ __device__ constexpr uint32_t idescN(int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
          ((uint32_t)(kTcRows >> 4) << 24);
@@ -137,14 +141,15 @@ __device__ __forceinline__ void fenceProxyAsync() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-// two accumulator buffers of up to 96 FP32 columns, 128 apart
-__device__ __forceinline__ void tmemAlloc256(uint32_t slot) {
-  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(slot)
+// the whole tensor memory (one CTA per SM): two accumulator buffers x two
+// k-step chains of up to 96 FP32 columns, buffer b chain c at column 128 b + 256 c
+__device__ __forceinline__ void tmemAlloc512(uint32_t slot) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(slot)
                : "memory");
   asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
 }
-__device__ __forceinline__ void tmemDealloc256(uint32_t taddr) {
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(taddr) : "memory");
+__device__ __forceinline__ void tmemDealloc512(uint32_t taddr) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(taddr) : "memory");
 }
 __device__ __forceinline__ void tcFenceBefore() {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -238,16 +243,19 @@ __global__ void __launch_bounds__(256) tcFillKernel(TcFill const *__restrict__ f
 
 // Persistent CTA over its chunk stream (one apply stage, one tile of 16 RHS),
 // warp-specialised around mbarriers:
-//   warp 4 (lane 0)  bulk-copies the A planes of chunk i into stage i % 3
+//   warp 8 (lane 0)  bulk-copies the A planes of chunk i into stage i % 3
 //                    once the MMAs of chunk i-3 are done (empty);
-//   warps 0-3        build the bf16 B planes of chunk i from registers loaded
-//                    one chunk ahead (fullB), then read chunk i-1's partial
-//                    sums from TMEM (accFull) into FP32 registers, release
-//                    the TMEM buffer (accEmpty) and store finished items;
-//   warp 5 (lane 0)  issues chunk i's MMAs into TMEM buffer i % 2 once its A
-//                    and B planes have landed and the buffer was read.
-// Each chunk starts its TMEM buffer from zero, so the tensor cores accumulate
-// at most 16 k-steps x products before the sum moves to FP32 registers.
+//   warps 0-3        copy chunk i+2's FP32 right-hand sides into its stage
+//                    (cp.async) and build chunk i's bf16 B planes (fullB);
+//   warp 9 (lane 0)  issues chunk i's MMAs into TMEM buffer i % 2 once its A
+//                    and B planes have landed and the buffer was read;
+//   warps 4-7        read each chunk's partial sums from TMEM (accFull) into
+//                    FP32 registers, release the buffer (accEmpty) and store
+//                    finished items.
+// Each chunk starts its TMEM buffer from zero and alternates its k-steps
+// between two accumulator chains, so the tensor cores accumulate at most 4
+// k-steps before the sums move to FP32 registers (the tensor-core FP32
+// accumulation loses accuracy over long chains).
 // Every wait is bounded (kWaitLimitNs) and gives up when another role has;
 // the CTA then waits (bounded) for the copies and MMAs it has in flight,
 // frees its TMEM and reports kStatusTcTimeout.
@@ -282,12 +290,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
     }
     for (int b = 0; b < 2; ++b) {
       mbarInit(accFull + 8 * b, 1);
-      mbarInit(accEmpty + 8 * b, kBuilders / 32);
+      mbarInit(accEmpty + 8 * b, kExtractors / 32);
     }
     *abortFlag = 0;
     fenceMbarInit();
   }
-  if (warp == kMmaWarp) tmemAlloc256(smemAddr(tmemSlot));
+  if (warp == kMmaWarp) tmemAlloc512(smemAddr(tmemSlot));
   tcFenceBefore();
   __syncthreads();
   tcFenceAfter();
@@ -347,15 +355,26 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
         uint32_t const aS = sbase + s * L::stageBytes, bS = aS + L::aBytes;
         uint32_t const lboA = (uint32_t)mg * 128;
         int const ksteps = (kg + 1) >> 1;
-        for (int st = 0; st < ksteps; ++st) {
-          // A plane t times the B planes 0 .. TERMS-1-t, side by side in N:
-          // D columns 32 u .. 32 u + 31 collect the products with B plane u
-          uint64_t const db = smemDesc(bS + 2 * st * kBKGroupBytes, kBKGroupBytes, 128);
+        // A plane t times the B planes 0 .. TERMS-1-t, side by side in N: D
+        // columns 32 u .. 32 u + 31 collect the products with B plane u.  The
+        // descriptors of k-step st are those of k-step 0 with the start
+        // address advanced (the address field is the low 14 bits, in 16 B).
+        uint64_t da[TERMS];
+#pragma unroll
+        for (int t = 0; t < TERMS; ++t) da[t] = smemDesc(aS + t * kAPlaneBytes, lboA, 128);
+        uint64_t db = smemDesc(bS, kBKGroupBytes, 128);
+        uint64_t const stepA = (2 * lboA) >> 4, stepB = (2 * kBKGroupBytes) >> 4;
+        uint32_t const d = tmem + 128 * b;
+#pragma unroll
+        for (int st = 0; st < kTcChunkCols / 8; ++st) {
+          if (st >= ksteps) break;
+          uint32_t const dc = d + 256 * (st & 1);   // even / odd k-step chain
 #pragma unroll
           for (int t = 0; t < TERMS; ++t) {
-            uint64_t const da = smemDesc(aS + t * kAPlaneBytes + 2 * st * lboA, lboA, 128);
-            tcMma(tmem + 128 * b, da, db, idescN(kTcN * (TERMS - t)), (st | t) ? 1u : 0u);
+            tcMma(dc, da[t], db, idescN(kTcN * (TERMS - t)), (st >= 2 || t > 0) ? 1u : 0u);
+            da[t] += stepA;
           }
+          db += stepB;
         }
         tcCommit(empty + 8 * s);
         tcCommit(accFull + 8 * b);
@@ -367,141 +386,155 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
         mbarDrain(empty + 8 * (last % S), (uint32_t)((last / S) & 1));
     }
   } else {
-    // ---- B planes, partial sums, stores ----
-    // Half h = tid / 128 of the builders converts the k-steps st = h, h+2, ..
-    // Element (j, q) of a k-step's 8 columns x 16 RHS belongs to one thread
-    // of the half: j = 8 st + (lane & 3) + 4 (w & 1), q = (lane >> 2) + 8 (w >> 1)
-    // with w = its warp within the half, so a warp's B stores fall in 32
-    // distinct banks.  The thread that copies an element into the X stage is
-    // the one that converts it, so the cp.async groups need no barrier.
-    // For the partial sums half h takes RHS 8h .. 8h+7 of TMEM lane quarter w.
-    int const h = tid >> 7, w = warp & 3;
-    int const jOff = (lane & 3) + 4 * (w & 1), q = (lane >> 2) + 8 * (w >> 1);
-    float acc[kTcRhs];   // RHS 8h .. 8h+7: real parts, then imaginary parts
-#pragma unroll
-    for (int c = 0; c < kTcRhs; ++c) acc[c] = 0.f;
-    // chunk descriptors live in registers from one iteration before their
-    // first use (the cp.async of the chunk's inputs) to their last (its store)
-    struct Cd {
-      int64_t inRow, outRow;
-      int32_t nc, kg, mg, rows, inIsX, flags;
+    struct Cd {            // builders: inputs of a chunk
+      int64_t inRow;
+      int32_t nc, kg, mg, inIsX;
     };
     auto loadCd = [&](int64_t i) {
       Cd d{};
       if (i < nCh) {
         TcChunk const &k = ch[i];
-        d = Cd{k.inRow, k.outRow, k.nc, k.kg, k.mg, k.rows, k.inIsX, k.flags};
+        d = Cd{k.inRow, k.nc, k.kg, k.mg, k.inIsX};
       }
       return d;
     };
-    auto issueX = [&](Cd const &d, int64_t i) {
-      int64_t const xld = d.inIsX ? ldx : R;
-      float2 const *src = (d.inIsX ? X : W) + d.inRow * xld + r0 + q;
-      uint32_t const xs = sbase + (int)(i % S) * L::stageBytes + L::aBytes + L::bBytes;
-      if (q < nr)
-        for (int j = 8 * h + jOff; j < d.nc; j += 16)
-          cpAsync8(xs + (uint32_t)(j * kTcRhs + q) * 8, src + (int64_t)j * xld);
+    struct Ce {            // extractors: outputs of a chunk
+      int64_t outRow;
+      int32_t rows, kg, flags;
     };
-    // TMEM partial sums of chunk j into acc; stores the item after its last chunk
-    auto extract = [&](Cd const &d, int64_t j) -> bool {
-      int const b = (int)(j & 1);
-      if (!mbarWait(accFull + 8 * b, (uint32_t)((j >> 1) & 1), abortFlag)) return false;
-      tcFenceAfter();
-      uint32_t const tl = tmem + 128 * b + 8 * h + ((uint32_t)(w * 32) << 16);
-      float v[TERMS][kTcRhs];
-#pragma unroll
-      for (int u = 0; u < TERMS; ++u) {
-        tmemLoad8(tl + 32 * u, v[u]);                  // real parts
-        tmemLoad8(tl + 32 * u + kTcRhs, v[u] + 8);     // imaginary parts
+    auto loadCe = [&](int64_t i) {
+      Ce d{};
+      if (i < nCh) {
+        TcChunk const &k = ch[i];
+        d = Ce{k.outRow, k.rows, k.kg, k.flags};
       }
-      tmemWaitLoads();
-#pragma unroll
-      for (int c = 0; c < kTcRhs; ++c) {
-        float t = v[TERMS - 1][c];   // products with the smallest B plane first
-#pragma unroll
-        for (int u = TERMS - 2; u >= 0; --u) t += v[u][c];
-        acc[c] += t;
-      }
-      tcFenceBefore();
-      __syncwarp();
-      if (lane == 0) mbarArrive(accEmpty + 8 * b);
-      if (d.flags & kTcLast) {
-        int const row = w * 32 + lane;
-        if (row < d.rows) {
-          float2 *out = W + (d.outRow + row) * R + r0 + 8 * h;
-#pragma unroll
-          for (int c = 0; c < 8; ++c)
-            if (8 * h + c < nr) out[c] = make_float2(acc[c], acc[8 + c]);
-        }
-#pragma unroll
-        for (int c = 0; c < kTcRhs; ++c) acc[c] = 0.f;
-      }
-      return true;
+      return d;
     };
-    Cd dPrev{}, d0 = loadCd(0), d1 = loadCd(1), d2 = loadCd(2);
-    // inputs of chunks 0 and 1 in flight before the loop (two cp.async groups)
-    if (0 < nCh) issueX(d0, 0);
-    cpAsyncCommit();
-    if (1 < nCh) issueX(d1, 1);
-    cpAsyncCommit();
-    bool ok = true;
-    for (int64_t i = 0; i < nCh && ok; ++i) {
-      int const s = (int)(i % S);
-      Cd const d3 = loadCd(i + 3);   // used from the next iteration on
-      // inputs of chunk i+2 into its stage: that stage's X area last held
-      // chunk i-1, which this thread has converted
-      if (i + 2 < nCh) issueX(d2, i + 2);
+    if (tid < kBuilders) {
+      // ---- B planes ----
+      // Element (j, q) of a k-step's 8 columns x 16 RHS belongs to one
+      // builder: j = 8 st + (lane & 3) + 4 (warp & 1), q = (lane >> 2) +
+      // 8 (warp >> 1), so a warp's B stores fall in 32 distinct banks.  The
+      // thread that copies an element into the X stage is the one that
+      // converts it, so the cp.async groups need no barrier.  Descriptors are
+      // loaded one iteration before their first use.
+      int const jOff = (lane & 3) + 4 * (warp & 1), q = (lane >> 2) + 8 * (warp >> 1);
+      auto issueX = [&](Cd const &d, int64_t i) {
+        int64_t const xld = d.inIsX ? ldx : R;
+        float2 const *src = (d.inIsX ? X : W) + d.inRow * xld + r0 + q;
+        uint32_t const xs = sbase + (int)(i % S) * L::stageBytes + L::aBytes + L::bBytes;
+        if (q < nr)
+          for (int j = jOff; j < d.nc; j += 8)
+            cpAsync8(xs + (uint32_t)(j * kTcRhs + q) * 8, src + (int64_t)j * xld);
+      };
+      Cd d0 = loadCd(0), d1 = loadCd(1), d2 = loadCd(2);
+      // inputs of chunks 0 and 1 in flight before the loop (two cp.async groups)
+      if (0 < nCh) issueX(d0, 0);
       cpAsyncCommit();
-      if (i >= S && !mbarWait(empty + 8 * s, (uint32_t)((i / S - 1) & 1), abortFlag)) {
-        ok = false;
-        break;
-      }
-      cpAsyncWait<2>();   // this thread's elements of chunk i have landed
-      uint8_t *stage = smem + s * L::stageBytes;
-      uint8_t *bsm = stage + L::aBytes;
-      float2 const *xs = reinterpret_cast<float2 const *>(stage + L::aBytes + L::bBytes);
-      int const ksteps = (d0.kg + 1) >> 1;
-      for (int st = h; st < ksteps; st += 2) {
-        int const j = 8 * st + jOff;
-        float2 const v = (j < d0.nc && q < nr) ? xs[j * kTcRhs + q] : make_float2(0.f, 0.f);
-        uint32_t pr[TERMS];
-        splitPair<TERMS>(v.x, v.y, pr);
-        int const kk = 2 * j;
-        uint32_t const offRe =
-            (kk >> 3) * kBKGroupBytes + (q >> 3) * 128 + (q & 7) * 16 + (kk & 7) * 2;
-        uint32_t const offIm = offRe + 2 * 128;   // column 16 + q: two core rows further
+      if (1 < nCh) issueX(d1, 1);
+      cpAsyncCommit();
+      for (int64_t i = 0; i < nCh; ++i) {
+        int const s = (int)(i % S);
+        Cd const d3 = loadCd(i + 3);   // used from the next iteration on
+        // inputs of chunk i+2 into its stage: that stage's X area last held
+        // chunk i-1, which this thread has converted
+        if (i + 2 < nCh) issueX(d2, i + 2);
+        cpAsyncCommit();
+        if (i >= S && !mbarWait(empty + 8 * s, (uint32_t)((i / S - 1) & 1), abortFlag)) {
+          *abortFlag = 1;
+          break;
+        }
+        cpAsyncWait<2>();   // this thread's elements of chunk i have landed
+        uint8_t *stage = smem + s * L::stageBytes;
+        uint8_t *bsm = stage + L::aBytes;
+        float2 const *xs = reinterpret_cast<float2 const *>(stage + L::aBytes + L::bBytes);
+        int const ksteps = (d0.kg + 1) >> 1;
+        for (int st = 0; st < ksteps; ++st) {
+          int const j = 8 * st + jOff;
+          float2 const v = (j < d0.nc && q < nr) ? xs[j * kTcRhs + q] : make_float2(0.f, 0.f);
+          uint32_t pr[TERMS];
+          splitPair<TERMS>(v.x, v.y, pr);
+          int const kk = 2 * j;
+          uint32_t const offRe =
+              (kk >> 3) * kBKGroupBytes + (q >> 3) * 128 + (q & 7) * 16 + (kk & 7) * 2;
+          uint32_t const offIm = offRe + 2 * 128;   // column 16 + q: two core rows further
 #pragma unroll
-        for (int t = 0; t < TERMS; ++t) {
-          // rows 2j, 2j+1 of column q: (Re x, -Im x); of column 16+q: (Im x, Re x)
-          *reinterpret_cast<uint32_t *>(bsm + t * 512 + offRe) = pr[t] ^ 0x80000000u;
-          *reinterpret_cast<uint32_t *>(bsm + t * 512 + offIm) = __byte_perm(pr[t], 0, 0x1032);
+          for (int t = 0; t < TERMS; ++t) {
+            // rows 2j, 2j+1 of column q: (Re x, -Im x); of column 16+q: (Im x, Re x)
+            *reinterpret_cast<uint32_t *>(bsm + t * 512 + offRe) = pr[t] ^ 0x80000000u;
+            *reinterpret_cast<uint32_t *>(bsm + t * 512 + offIm) =
+                __byte_perm(pr[t], 0, 0x1032);
+          }
+        }
+        // an odd k-group count leaves the second half of the last k-step unset
+        // in A: zero it (B is zero there, but stale shared memory may hold NaNs)
+        if (d0.kg & 1) {
+          uint32_t const padOff = (uint32_t)d0.kg * d0.mg * 128, padBytes = (uint32_t)d0.mg * 128;
+          for (uint32_t e = (uint32_t)tid * 16; e < padBytes; e += kBuilders * 16)
+#pragma unroll
+            for (int t = 0; t < TERMS; ++t)
+              *reinterpret_cast<uint4 *>(stage + t * kAPlaneBytes + padOff + e) =
+                  make_uint4(0, 0, 0, 0);
+        }
+        fenceProxyAsync();
+        __syncwarp();
+        if (lane == 0) mbarArrive(fullB + 8 * s);
+        d0 = d1;
+        d1 = d2;
+        d2 = d3;
+      }
+      cpAsyncWait<0>();
+    } else {
+      // ---- TMEM partial sums, FP32 accumulation, stores ----
+      // extractor warp e reads TMEM lane quarter e: item row 32 e + lane
+      int const e = warp & 3;
+      float acc[2 * kTcRhs];   // RHS 0..15 real parts, then imaginary parts
+#pragma unroll
+      for (int c = 0; c < 2 * kTcRhs; ++c) acc[c] = 0.f;
+      Ce dn = loadCe(0);
+      for (int64_t j = 0; j < nCh; ++j) {
+        Ce const d = dn;
+        dn = loadCe(j + 1);
+        int const b = (int)(j & 1);
+        if (!mbarWait(accFull + 8 * b, (uint32_t)((j >> 1) & 1), abortFlag)) {
+          *abortFlag = 1;
+          break;
+        }
+        tcFenceAfter();
+        uint32_t const tl = tmem + 128 * b + ((uint32_t)(e * 32) << 16);
+        int const chains = d.kg > 2 ? 2 : 1;   // the odd k-step chain was written
+        for (int c = 0; c < chains; ++c) {
+#pragma unroll
+          for (int part = 0; part < 4; ++part) {   // columns 8 part .. 8 part + 7 of each group
+            float v[TERMS][8];
+#pragma unroll
+            for (int u = 0; u < TERMS; ++u) tmemLoad8(tl + 256 * c + 32 * u + 8 * part, v[u]);
+            tmemWaitLoads();
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+              float t = v[TERMS - 1][k];   // products with the smallest B plane first
+#pragma unroll
+              for (int u = TERMS - 2; u >= 0; --u) t += v[u][k];
+              acc[8 * part + k] += t;
+            }
+          }
+        }
+        tcFenceBefore();
+        __syncwarp();
+        if (lane == 0) mbarArrive(accEmpty + 8 * b);
+        if (d.flags & kTcLast) {
+          int const row = e * 32 + lane;
+          if (row < d.rows) {
+            float2 *out = W + (d.outRow + row) * R + r0;
+#pragma unroll
+            for (int c = 0; c < kTcRhs; ++c)
+              if (c < nr) out[c] = make_float2(acc[c], acc[kTcRhs + c]);
+          }
+#pragma unroll
+          for (int c = 0; c < 2 * kTcRhs; ++c) acc[c] = 0.f;
         }
       }
-      // an odd k-group count leaves the second half of the last k-step unset
-      // in A: zero it (B is zero there, but stale shared memory may hold NaNs)
-      if (d0.kg & 1) {
-        uint32_t const padOff = (uint32_t)d0.kg * d0.mg * 128, padBytes = (uint32_t)d0.mg * 128;
-        for (uint32_t e = (uint32_t)tid * 16; e < padBytes; e += kBuilders * 16)
-#pragma unroll
-          for (int t = 0; t < TERMS; ++t)
-            *reinterpret_cast<uint4 *>(stage + t * kAPlaneBytes + padOff + e) =
-                make_uint4(0, 0, 0, 0);
-      }
-      fenceProxyAsync();
-      __syncwarp();
-      if (lane == 0) mbarArrive(fullB + 8 * s);
-      if (i >= 1 && !extract(dPrev, i - 1)) {
-        ok = false;
-        break;
-      }
-      dPrev = d0;
-      d0 = d1;
-      d1 = d2;
-      d2 = d3;
     }
-    if (ok) ok = extract(dPrev, nCh - 1);
-    cpAsyncWait<0>();
-    if (!ok) *abortFlag = 1;
   }
 
   tcFenceBefore();
@@ -509,7 +542,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
   if (warp == kMmaWarp) {
     __syncwarp();
     tcFenceAfter();
-    tmemDealloc256(tmem);
+    tmemDealloc512(tmem);
   }
   if (tid == 0 && *abortFlag) atomicOr(status, kStatusTcTimeout);
 }
