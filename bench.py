@@ -45,11 +45,13 @@ CONFIGS = {
 }
 METRIC = "Butterfly apply RHS/s at 1e-6 rel err vs plain FP64 GPU; GMRES time-to-1e-8"
 # DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
-# byte of each stage launch of the FP32 16-RHS apply, from one ncu capture of
-# the c2s workload; the c2 workload (same geometry, kernel and stage
-# structure at twice the size) reports its dominant launch's traffic as this
-# ratio times its own algorithmic bytes
-NCU_DRAM_PER_ALG = {("fp32", 16, 5): [0.7973, 1.0266, 0.9855, 0.7925]}
+# byte of each stage launch of the 16-RHS apply (FP32 pipelined kernel, bf16x3
+# tensor-core kernel), from one ncu capture of the c2s workload each; the c2
+# workload (same geometry, kernels and stage structure at twice the size)
+# reports its dominant launch's traffic as this ratio times its own
+# algorithmic bytes
+NCU_DRAM_PER_ALG = {("fp32", 16, 5): [0.7973, 1.0266, 0.9855, 0.7925],
+                    ("bf16x3", 16, 5): [0.8870, 1.0633, 1.0222, 0.9028]}
 ERR_BOUND = 1e-6
 
 
