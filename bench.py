@@ -1,7 +1,7 @@
 """Benchmark of the butterfly Helmholtz apply on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl bfg|reference]
-                    [--config c4|c2|c2s|c1] [--rhs R]
+                    [--config c4|c3|c3s|c2|c2s|c1] [--rhs R]
 
 One step = one apply of the factorization to R right-hand sides (the
 workload's synthetic, seeded inputs).  The metric is right-hand sides per
@@ -42,6 +42,13 @@ CONFIGS = {
     "c2s": dict(n=32768, k=256.0, curve="ellipse", a=3.0, b=2.0, leaf=64, tol=1e-10, R=16),
     # 262,144 / star r = 3 + 0.5 cos 5 theta, k=2048, tol 1e-7, 256 RHS
     "c4": dict(n=262144, k=2048.0, curve="star", a=3.0, b=3.0, leaf=64, tol=1e-7, R=256),
+    # 256 independent problems in one factorization and one apply: N log-uniform
+    # in [1,024, 16,384], sources iid uniform in [-1,1]^2, targets equispaced on
+    # the circle of radius 3, k = N / 30, leaf 64, tol 1e-8, 8 RHS (opt-in: its
+    # factors take ~63 GB in FP64 and minutes to build)
+    "c3": dict(batched=True, problems=256, nmin=1024, nmax=16384, leaf=64, tol=1e-8, R=8),
+    # the same at 64 problems, N in [1,024, 4,096] (seconds to build)
+    "c3s": dict(batched=True, problems=64, nmin=1024, nmax=4096, leaf=64, tol=1e-8, R=8),
 }
 METRIC = "Butterfly apply RHS/s at 1e-6 rel err vs plain FP64 GPU; GMRES time-to-1e-8"
 # DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
@@ -170,6 +177,145 @@ def max_over_ranks(v, dist):
 
 
 # ---------------------------------------------------------------------------
+# Batched problems
+# ---------------------------------------------------------------------------
+def batched_problems(B, cfg):
+    u = B.Rng(3).uniform(cfg["problems"])
+    lo, hi = np.log(cfg["nmin"]), np.log(cfg["nmax"])
+    sizes = np.floor(np.exp(lo + (hi - lo) * u)).astype(np.int64)
+    problems = [(B.uniform_square_points(int(n), 1000 + j), B.curve_points("circle", int(n), 3.0, 3.0))
+                for j, n in enumerate(sizes)]
+    return sizes, problems, sizes / 30.0
+
+
+def run_batched(args, cfg):
+    """--config c3: one batched factorization of all problems; a step is one
+    apply of R RHS to every problem at once (the block-diagonal operator)."""
+    import torch
+
+    import butterfly_gb300 as B
+    world, rank, local, dist = dist_setup()
+    torch.cuda.set_device(local)
+    ctx = B.Context(local)
+    sizes, problems, ks = batched_problems(B, cfg)
+    t0 = time.perf_counter()
+    fac = B.make_batched(B.Helm2(1.0), problems, ks, leaf_size=cfg["leaf"], rank_eps=cfg["tol"],
+                         pinv_tol=cfg["tol"], context=ctx)
+    fac_s = time.perf_counter() - t0
+    n = int(sizes.sum())
+    R = args.rhs or cfg["R"]
+    so, to = fac.src_offsets, fac.tgt_offsets
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    Xh = B.Rng(1234 + rank).complex_randn(n * R).reshape(n, R)     # original point order
+    with torch.cuda.stream(stream):
+        X64 = torch.from_numpy(Xh).to("cuda")
+        X32 = X64.to(torch.complex64)
+        Y64 = torch.empty((n, R), dtype=torch.complex128, device="cuda")
+        Y32 = torch.empty((n, R), dtype=torch.complex64, device="cuda")
+    stream.synchronize()
+    precs = {"fp64": (X64, Y64), "fp32": (X32, Y32), "bf16x3": (X32, Y32), "bf16x2": (X32, Y32)}
+    # dense FP64 rows of 8 sampled problems (64 target rows each)
+    ref = []
+    for j in range(0, len(problems), max(1, len(problems) // 8)):
+        src, tgt = problems[j]
+        rows = np.unique(np.linspace(0, len(tgt) - 1, 64).astype(np.int64))
+        K = B.kernel_matrix(B.Helm2(float(ks[j])), src, tgt[rows], context=ctx)
+        ref.append((to[j] + rows, K @ Xh[so[j]:so[j + 1]]))
+    errs = {}
+    for p, (X, Y) in precs.items():
+        fac.apply_device(X.data_ptr(), R, R, Y.data_ptr(), R, p, original_order=True)
+        stream.synchronize()
+        Yh = Y.cpu().numpy().astype(np.complex128)
+        num = sum(float(np.linalg.norm(Yh[r] - yd) ** 2) for r, yd in ref)
+        den = sum(float(np.linalg.norm(yd) ** 2) for r, yd in ref)
+        errs[p] = (num / den) ** 0.5
+
+    def timed(p):
+        X, Y = precs[p]
+        for _ in range(max(3, args.warmup)):
+            fac.apply_device(X.data_ptr(), R, R, Y.data_ptr(), R, p)
+        stream.synchronize()
+        barrier(dist)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fac.apply_device(X.data_ptr(), R, R, Y.data_ptr(), R, p)
+        e1.record(stream)
+        e1.synchronize()
+        barrier(dist)
+        return e0.elapsed_time(e1)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    total_ms = {p: max_over_ranks(timed(p), dist) for p in precs}
+    clk = clocks.stop()
+    rhs_s = {p: world * R * args.steps / (total_ms[p] / 1e3) for p in precs}
+    ok = [p for p in precs if errs[p] <= ERR_BOUND]
+    head = max(ok, key=lambda p: rhs_s[p]) if ok else "fp64"
+    X, Y = precs[head]
+    per = np.mean([fac.apply_timed(X.data_ptr(), R, R, Y.data_ptr(), R, head) for _ in range(3)],
+                  axis=0)
+    info = fac.launch_info()
+    dom = int(np.argmax(per))
+    sA = {"fp64": 16, "fp32": 8, "bf16x3": 12, "bf16x2": 8}[head]
+    sv = 16 if head == "fp64" else 8
+    alg = float(info[dom, 0] * sA + R * sv * (info[dom, 1] + info[dom, 2]))
+    try:
+        peak, peak_src = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        peak, peak_src = 6800.0, "fallback"
+    achieved = alg / (per[dom] / 1e3) / 1e9
+    # end to end with host complex128 operands
+    Xp = torch.from_numpy(Xh).pin_memory()
+    Yp = torch.empty((n, R), dtype=torch.complex128).pin_memory()
+    lib = B.lib()
+    ctx.check(lib.bfgFacApplyHost(fac.handle, B.PRECISIONS[head], B._VP(Xp.data_ptr()), R, R,
+                                  B._VP(Yp.data_ptr()), R, 0))
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 10))
+    for _ in range(e2e_steps):
+        ctx.check(lib.bfgFacApplyHost(fac.handle, B.PRECISIONS[head], B._VP(Xp.data_ptr()), R, R,
+                                      B._VP(Yp.data_ptr()), R, 0))
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
+    if rank != 0:
+        return
+    st = fac.stats()
+    line = {"metric": METRIC, "value": rhs_s[head], "unit": "RHS/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms[head] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": {"fp64": "complex128", "fp32": "complex64",
+                      "bf16x3": "bf16x3 split (complex64 vectors)",
+                      "bf16x2": "bf16x2 split (complex64 vectors)"}[head],
+            "data": "synthetic",
+            "config": {"workload": "helmholtz2d_butterfly_batched_%d" % cfg["problems"],
+                       "problems": cfg["problems"], "n_min": int(sizes.min()),
+                       "n_max": int(sizes.max()), "n_total": n, "k": "N/30",
+                       "targets": "circle r=3", "leaf_size": cfg["leaf"],
+                       "tolerance": cfg["tol"], "rhs": R,
+                       "l2": "factor arena and vectors larger than L2 (129 MB); no flush needed"},
+            "precision": head, "rel_err": errs[head], "rel_err_all": errs,
+            "rhs_per_s_all": rhs_s, "problem_rhs_per_s": rhs_s[head] * cfg["problems"],
+            "err_bound": ERR_BOUND, "err_sample": "64 rows of each of %d problems" % len(ref),
+            "factorization": {"wall_s": fac_s, "device_ms": st["factorMs"],
+                              "blocks": st["numBlocks"], "bytes_fp64": fac.num_bytes(),
+                              "max_rank": st["maxRank"]},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
+                         "kernel": "apply launch %d of %d" % (dom, len(per)),
+                         "launch_ms": float(per[dom]), "alg_bytes": alg},
+            "cpu_baseline": None,
+            "e2e": {"value": world * R * e2e_steps / e2e_s, "unit": "RHS/s",
+                    "h2d_bytes_per_step": n * R * 16, "d2h_bytes_per_step": n * R * 16,
+                    "precision": head},
+            "clocks": clk, "gpu_launches": len(info) * args.steps}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
 # GMRES time-to-1e-8 (the metric's second part)
 # ---------------------------------------------------------------------------
 def gmres_scattering(B, ctx):
@@ -290,6 +436,15 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 def main():
     args = parse()
+    if CONFIGS[args.config].get("batched"):
+        if args.impl == "reference":
+            if int(os.environ.get("RANK", "0")) == 0:
+                print(json.dumps({"impl": "reference", "unavailable":
+                                  "the batched workload has no CPU reference timing here "
+                                  "(256 CPU factorizations take hours)"}))
+            return
+        run_batched(args, CONFIGS[args.config])
+        return
     if args.impl == "reference":
         run_reference(args)
         return
