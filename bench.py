@@ -267,7 +267,7 @@ def run_batched(args, cfg):
         peak, peak_src = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         peak, peak_src = 6800.0, "fallback"
-    achieved = alg / (per[dom] / 1e3) / 1e9
+    achieved = float(alg / (float(per[dom]) / 1e3) / 1e9)
     # end to end with host complex128 operands
     Xp = torch.from_numpy(Xh).pin_memory()
     Yp = torch.empty((n, R), dtype=torch.complex128).pin_memory()
