@@ -20,6 +20,7 @@
 
 #include <cooperative_groups.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -969,9 +970,19 @@ cudaError_t launchApplyStage(ApplyItem const *items, int64_t nItems,
                                                                           arena, X, ldx, W);
   } else if (R > 8 && !forceTileKernel()) {
     size_t const smem = 2 * PipeShape<T2>::stageBytes;
-    cudaError_t e = cudaFuncSetAttribute(applyPipeKernel<T2, kPipeWarps, 2>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // the shared-memory limit is a per-device function attribute: set it once
+    // per device, so that applies enqueue nothing else (stream capture)
+    static std::atomic<uint64_t> attrSet{0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
+    uint64_t const bit = 1ull << (dev & 63);
+    if (!(attrSet.load() & bit)) {
+      e = cudaFuncSetAttribute(applyPipeKernel<T2, kPipeWarps, 2>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      attrSet.fetch_or(bit);
+    }
     dim3 grid((unsigned)nItems, (unsigned)((R + 15) / 16));
     applyPipeKernel<T2, kPipeWarps, 2><<<grid, 32 * kPipeWarps, smem, stream>>>(
         items, contribs, arena, X, ldx, W, R);
