@@ -87,6 +87,8 @@ def lib() -> ctypes.CDLL:
         "bfgFacHelm2MakeBatched": [_VP, ctypes.POINTER(_Helm2C), _VP, _I64, _VP, _VP, _VP, _VP,
                                    _VP, _VP, ctypes.POINTER(_FacOptionsC), ctypes.POINTER(_VP)],
         "bfgFacDestroy": [_VP],
+        "bfgFacSave": [_VP, ctypes.c_char_p],
+        "bfgFacLoad": [_VP, ctypes.c_char_p, ctypes.POINTER(_VP)],
         "bfgFacGetShape": [_VP, ctypes.POINTER(_I64), ctypes.POINTER(_I64)],
         "bfgFacGetPerms": [_VP, _VP, _VP],
         "bfgFacNumBytes": [_VP, ctypes.POINTER(_I64)],
@@ -381,6 +383,11 @@ class Fac:
         return tab, ent
 
     # -- apply -------------------------------------------------------------
+    def save(self, path: str):
+        """Writes the factorization (inputs and FP64 factors) to ``path``;
+        ``load_fac`` rebuilds it without factorizing again."""
+        self.ctx.check(lib().bfgFacSave(self.handle, os.fsencode(path)), "save")
+
     def apply(self, X, precision: str = "fp64", original_order: bool = False):
         """Y = A X.  numpy complex128 X -> host path (copies inside);
         torch CUDA X -> device path on the context's stream."""
@@ -453,6 +460,15 @@ class Fac:
                                                  _VP(X_dev.data_ptr()), R, R,
                                                  _VP(out.data_ptr()), R), "dense_rows")
         return out
+
+
+def load_fac(path: str, helm: Helm2 | None = None, context: Context | None = None) -> "Fac":
+    """A factorization saved by ``Fac.save``, rebuilt on the context's GPU
+    (bfgFacLoad).  ``helm`` only labels the Python object."""
+    ctx = context or default_context()
+    h = _VP()
+    ctx.check(lib().bfgFacLoad(ctx.handle, os.fsencode(path), ctypes.byref(h)), "load")
+    return Fac(ctx, h, helm)
 
 
 def kernel_matrix(helm: Helm2, src, tgt, src_normals=None, tgt_normals=None,

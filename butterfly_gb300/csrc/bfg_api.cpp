@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -91,6 +92,10 @@ struct bfgFac_s {
     DevBuf chunks, ctaChunk0, arena;
   } tc[2];
   DevBuf tcStatus;                  // kStatusTcTimeout from the tensor-core kernel
+  // the inputs (original order), kept for bfgFacSave; k holds one
+  // wavenumber per problem and the offsets are empty for a single problem
+  std::vector<double> inSrcXy, inSrcN, inTgtXy, inTgtN, inK;
+  std::vector<int64_t> inSrcOff, inTgtOff;
 };
 
 namespace {
@@ -422,6 +427,20 @@ void ensureArena32(bfgFac f) {
   f->arena32Ready = true;
 }
 
+void keepInputs(bfgFac f, double const *srcXy, double const *srcN, int64_t nSrc,
+                double const *tgtXy, double const *tgtN, int64_t nTgt, double const *k,
+                int64_t numProblems, int64_t const *srcOff, int64_t const *tgtOff) {
+  f->inSrcXy.assign(srcXy, srcXy + 2 * nSrc);
+  f->inTgtXy.assign(tgtXy, tgtXy + 2 * nTgt);
+  if (srcN) f->inSrcN.assign(srcN, srcN + 2 * nSrc);
+  if (tgtN) f->inTgtN.assign(tgtN, tgtN + 2 * nTgt);
+  f->inK.assign(k, k + numProblems);
+  if (srcOff) {
+    f->inSrcOff.assign(srcOff, srcOff + numProblems + 1);
+    f->inTgtOff.assign(tgtOff, tgtOff + numProblems + 1);
+  }
+}
+
 bool isTcPrecision(bfgPrecision p) {
   return p == BFG_PRECISION_BF16X2 || p == BFG_PRECISION_BF16X3;
 }
@@ -596,6 +615,39 @@ bfgStatus noAllocApplyFp64(bfgFac f, double2 const *X, int64_t ldx, int64_t R, d
 
 }  // namespace bfg
 
+namespace {
+
+// On-disk factorization: this header, then the wavenumbers (numProblems), the
+// problem offsets (batched only, numProblems + 1 each), source xy, source
+// normals (if any), target xy, target normals (if any), and the FP64 factor
+// arena (arenaEntries complex128 values in plan order).  All little-endian,
+// written as laid out in memory (the same layout on x86-64 and aarch64).
+constexpr char kFacMagic[8] = {'B', 'F', 'G', 'F', 'A', 'C', '\0', '\1'};
+constexpr uint32_t kFacVersion = 1;
+
+struct FacFileHeader {
+  char magic[8];
+  uint32_t version, reserved;
+  bfgHelm2 helm;
+  bfgFacOptions opts;
+  int64_t numProblems;
+  int32_t batched, srcHasNormals, tgtHasNormals, reserved2;
+  int64_t nSrc, nTgt, arenaEntries;
+};
+static_assert(sizeof(FacFileHeader) == 144, "file header layout");
+
+constexpr int64_t kFileChunkEntries = int64_t(1) << 24;   // 256 MB of complex128
+
+void writeAll(FILE *fp, void const *p, size_t n) {
+  if (n && std::fwrite(p, 1, n, fp) != n) throw BfgError{BFG_ERROR_RUNTIME, "save: write failed"};
+}
+void readAll(FILE *fp, void *p, size_t n) {
+  if (n && std::fread(p, 1, n, fp) != n)
+    throw BfgError{BFG_ERROR_RUNTIME, "load: file truncated"};
+}
+
+}  // namespace
+
 extern "C" {
 
 bfgStatus bfgContextCreate(int32_t device, bfgContext *out) {
@@ -690,6 +742,8 @@ bfgStatus bfgFacHelm2MakeMultilevel(bfgContext ctx, bfgHelm2 const *helm, double
     f->ctx = ctx;
     f->helm = *helm;
     f->opts = o;
+    keepInputs(f, srcXy, srcNormals, numSrc, tgtXy, tgtNormals, numTgt, &helm->k, 1, nullptr,
+               nullptr);
     try {
       bfg::PlanParams pp;
       pp.k = helm->k;
@@ -759,6 +813,8 @@ bfgStatus bfgFacHelm2MakeBatched(bfgContext ctx, bfgHelm2 const *helm, double co
     f->helm = *helm;
     f->helm.k = k[0];
     f->opts = o;
+    keepInputs(f, srcXy, srcNormals, nSrc, tgtXy, tgtNormals, nTgt, k, numProblems, srcOffsets,
+               tgtOffsets);
     try {
       bfg::PlanParams pp;
       pp.leafSize = o.leafSize;
@@ -777,6 +833,158 @@ bfgStatus bfgFacHelm2MakeBatched(bfgContext ctx, bfgHelm2 const *helm, double co
     } catch (std::runtime_error const &e) {
       delete f;
       return fail(ctx, BFG_ERROR_RUNTIME, std::string("batched make: ") + e.what());
+    } catch (...) {
+      delete f;
+      throw;
+    }
+    *out = f;
+    return BFG_OK;
+  });
+}
+
+bfgStatus bfgFacSave(bfgFac f, char const *path) {
+  if (!f) return BFG_ERROR_INVALID_ARGUMENTS;
+  return guarded(f->ctx, [&]() -> bfgStatus {
+    if (!path) return fail(f->ctx, BFG_ERROR_INVALID_ARGUMENTS, "save: null path");
+    FILE *fp = std::fopen(path, "wb");
+    if (!fp) return fail(f->ctx, BFG_ERROR_RUNTIME, std::string("save: cannot open ") + path);
+    std::unique_ptr<FILE, int (*)(FILE *)> guard(fp, std::fclose);
+    FacFileHeader h{};
+    std::memcpy(h.magic, kFacMagic, sizeof h.magic);
+    h.version = kFacVersion;
+    h.helm = f->helm;
+    h.opts = f->opts;
+    h.numProblems = (int64_t)f->inK.size();
+    h.batched = f->inSrcOff.empty() ? 0 : 1;
+    h.srcHasNormals = f->inSrcN.empty() ? 0 : 1;
+    h.tgtHasNormals = f->inTgtN.empty() ? 0 : 1;
+    h.nSrc = (int64_t)f->inSrcXy.size() / 2;
+    h.nTgt = (int64_t)f->inTgtXy.size() / 2;
+    h.arenaEntries = f->plan.arenaEntries;
+    writeAll(fp, &h, sizeof h);
+    writeAll(fp, f->inK.data(), f->inK.size() * sizeof(double));
+    if (h.batched) {
+      writeAll(fp, f->inSrcOff.data(), f->inSrcOff.size() * sizeof(int64_t));
+      writeAll(fp, f->inTgtOff.data(), f->inTgtOff.size() * sizeof(int64_t));
+    }
+    writeAll(fp, f->inSrcXy.data(), f->inSrcXy.size() * sizeof(double));
+    writeAll(fp, f->inSrcN.data(), f->inSrcN.size() * sizeof(double));
+    writeAll(fp, f->inTgtXy.data(), f->inTgtXy.size() * sizeof(double));
+    writeAll(fp, f->inTgtN.data(), f->inTgtN.size() * sizeof(double));
+    ck(cudaStreamSynchronize(f->ctx->stream), "save");
+    std::vector<double2> buf((size_t)std::min(h.arenaEntries, kFileChunkEntries));
+    for (int64_t off = 0; off < h.arenaEntries; off += kFileChunkEntries) {
+      int64_t const n = std::min(kFileChunkEntries, h.arenaEntries - off);
+      ck(cudaMemcpy(buf.data(), f->arena64.as<double2>() + off, (size_t)n * sizeof(double2),
+                    cudaMemcpyDeviceToHost),
+         "save");
+      writeAll(fp, buf.data(), (size_t)n * sizeof(double2));
+    }
+    if (std::fclose(guard.release()) != 0)
+      return fail(f->ctx, BFG_ERROR_RUNTIME, "save: write failed");
+    return BFG_OK;
+  });
+}
+
+bfgStatus bfgFacLoad(bfgContext ctx, char const *path, bfgFac *out) {
+  if (!ctx) return BFG_ERROR_INVALID_ARGUMENTS;
+  return guarded(ctx, [&]() -> bfgStatus {
+    if (!path || !out) return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "load: null argument");
+    *out = nullptr;
+    FILE *fp = std::fopen(path, "rb");
+    if (!fp) return fail(ctx, BFG_ERROR_RUNTIME, std::string("load: cannot open ") + path);
+    std::unique_ptr<FILE, int (*)(FILE *)> guard(fp, std::fclose);
+    FacFileHeader h{};
+    readAll(fp, &h, sizeof h);
+    if (std::memcmp(h.magic, kFacMagic, sizeof h.magic) != 0 || h.version != kFacVersion)
+      return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "load: not a factorization file of this version");
+    int64_t const kMaxPoints = int64_t(1) << 34;
+    if (h.numProblems < 1 || h.nSrc < 1 || h.nTgt < 1 || h.nSrc > kMaxPoints ||
+        h.nTgt > kMaxPoints || h.arenaEntries < 0 || (h.batched != 0 && h.batched != 1) ||
+        (!h.batched && h.numProblems != 1) || h.numProblems > h.nSrc ||
+        !validLayerPot(h.helm.layerPot))
+      return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "load: inconsistent header");
+    auto *f = new bfgFac_s;
+    f->ctx = ctx;
+    f->helm = h.helm;
+    f->opts = h.opts;
+    try {
+      f->inK.resize((size_t)h.numProblems);
+      readAll(fp, f->inK.data(), f->inK.size() * sizeof(double));
+      if (h.batched) {
+        f->inSrcOff.resize((size_t)h.numProblems + 1);
+        f->inTgtOff.resize((size_t)h.numProblems + 1);
+        readAll(fp, f->inSrcOff.data(), f->inSrcOff.size() * sizeof(int64_t));
+        readAll(fp, f->inTgtOff.data(), f->inTgtOff.size() * sizeof(int64_t));
+        for (int64_t q = 0; q < h.numProblems; ++q)
+          if (f->inSrcOff[(size_t)q + 1] <= f->inSrcOff[(size_t)q] ||
+              f->inTgtOff[(size_t)q + 1] <= f->inTgtOff[(size_t)q])
+            throw BfgError{BFG_ERROR_INVALID_ARGUMENTS, "load: bad problem offsets"};
+        if (f->inSrcOff[0] != 0 || f->inTgtOff[0] != 0 ||
+            f->inSrcOff[(size_t)h.numProblems] != h.nSrc ||
+            f->inTgtOff[(size_t)h.numProblems] != h.nTgt)
+          throw BfgError{BFG_ERROR_INVALID_ARGUMENTS, "load: bad problem offsets"};
+      }
+      for (double kk : f->inK)
+        if (!(kk > 0)) throw BfgError{BFG_ERROR_INVALID_ARGUMENTS, "load: bad wavenumber"};
+      f->inSrcXy.resize((size_t)(2 * h.nSrc));
+      readAll(fp, f->inSrcXy.data(), f->inSrcXy.size() * sizeof(double));
+      if (h.srcHasNormals) {
+        f->inSrcN.resize((size_t)(2 * h.nSrc));
+        readAll(fp, f->inSrcN.data(), f->inSrcN.size() * sizeof(double));
+      }
+      f->inTgtXy.resize((size_t)(2 * h.nTgt));
+      readAll(fp, f->inTgtXy.data(), f->inTgtXy.size() * sizeof(double));
+      if (h.tgtHasNormals) {
+        f->inTgtN.resize((size_t)(2 * h.nTgt));
+        readAll(fp, f->inTgtN.data(), f->inTgtN.size() * sizeof(double));
+      }
+      // the plan is a deterministic function of the inputs: rebuild it and
+      // check it against the stored factors
+      bfg::PlanParams pp;
+      pp.leafSize = h.opts.leafSize;
+      pp.rankEps = h.opts.rankEps;
+      if (h.batched) {
+        bfg::makePlanBatched(f->plan, pp, f->inK.data(), f->inSrcXy.data(), f->inSrcOff.data(),
+                             f->inTgtXy.data(), f->inTgtOff.data(), h.numProblems);
+      } else {
+        pp.k = f->inK[0];
+        bfg::makePlan(f->plan, pp, f->inSrcXy.data(), h.nSrc, f->inTgtXy.data(), h.nTgt);
+      }
+      if (f->plan.arenaEntries != h.arenaEntries)
+        throw BfgError{BFG_ERROR_INVALID_ARGUMENTS,
+                       "load: the stored factors do not match the plan of the stored inputs"};
+      cudaStream_t s = ctx->stream;
+      f->srcHasNormals = h.srcHasNormals != 0;
+      f->tgtHasNormals = h.tgtHasNormals != 0;
+      uploadTreePoints(f->srcPts, f->inSrcXy.data(), h.srcHasNormals ? f->inSrcN.data() : nullptr,
+                       h.nSrc, f->plan.src.perm, s);
+      uploadTreePoints(f->tgtPts, f->inTgtXy.data(), h.tgtHasNormals ? f->inTgtN.data() : nullptr,
+                       h.nTgt, f->plan.tgt.perm, s);
+      upload(f->srcPerm, f->plan.src.perm, s, "perm");
+      upload(f->tgtPerm, f->plan.tgt.perm, s, "perm");
+      ck(cudaStreamSynchronize(s), "load");
+      ck(f->arena64.ensure((size_t)std::max<int64_t>(1, h.arenaEntries) * sizeof(double2)),
+         "arena");
+      std::vector<double2> buf((size_t)std::min(h.arenaEntries, kFileChunkEntries));
+      for (int64_t off = 0; off < h.arenaEntries; off += kFileChunkEntries) {
+        int64_t const n = std::min(kFileChunkEntries, h.arenaEntries - off);
+        readAll(fp, buf.data(), (size_t)n * sizeof(double2));
+        ck(cudaMemcpy(f->arena64.as<double2>() + off, buf.data(), (size_t)n * sizeof(double2),
+                      cudaMemcpyHostToDevice),
+           "load");
+      }
+      int64_t maxRank = 0;
+      for (auto const &b : f->plan.blocks) {
+        if (b.kind == bfg::kLast) maxRank = std::max<int64_t>(maxRank, b.n);
+        if (b.kind == bfg::kFirst || b.kind == bfg::kMiddle) maxRank = std::max<int64_t>(maxRank, b.m);
+      }
+      f->stats.maxRank = maxRank;
+      buildApply(f);
+      fillStats(f);
+    } catch (std::runtime_error const &e) {
+      delete f;
+      return fail(ctx, BFG_ERROR_RUNTIME, std::string("load: ") + e.what());
     } catch (...) {
       delete f;
       throw;

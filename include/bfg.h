@@ -139,6 +139,22 @@ bfgStatus bfgFacHelm2MakeBatched(bfgContext ctx, bfgHelm2 const *helm, double co
                                  double const *tgtXy, double const *tgtNormals,
                                  int64_t const *tgtOffsets, bfgFacOptions const *opts,
                                  bfgFac *fac);
+/* Writes the factorization to `path`: its inputs (points, normals,
+ * wavenumbers, options, problem offsets) and its FP64 factors.  The
+ * reference's dumps (bfMatDump, mat.c:67-73; bf_one_block.c:166-258) store
+ * block values without what rebuilds the operator, so there is no
+ * counterpart; this caches factorizations that take minutes to build.
+ * Synchronises the context's stream.  Little-endian; files move between the
+ * x86-64 and aarch64 builds. */
+bfgStatus bfgFacSave(bfgFac fac, char const *path);
+/* Rebuilds a factorization saved by bfgFacSave on ctx's device without
+ * factorizing again: the plan (trees, ranks, block order) is rebuilt on the
+ * host from the stored inputs -- it is a deterministic function of them --
+ * and must account for exactly the stored number of factor entries; the
+ * factors are then uploaded.  BFG_ERROR_INVALID_ARGUMENTS for a file of
+ * another format or version or with inconsistent contents,
+ * BFG_ERROR_RUNTIME for I/O failures. */
+bfgStatus bfgFacLoad(bfgContext ctx, char const *path, bfgFac *fac);
 /* bfMatDelete on the factorization (mat.h:57). */
 bfgStatus bfgFacDestroy(bfgFac fac);
 /* bfMatGetNumRows / bfMatGetNumCols (mat.c). */
