@@ -52,14 +52,32 @@ void Quadtree::build(double const *xy, int64_t n, int64_t leafSize_) {
     ymax = std::fmax(ymax, py[i]);
   }
   double w = xmax - xmin, h = ymax - ymin;
-  if (w > h) {
+  // the reference's formula divides by a zero side for one point or for
+  // collinear points (its boxes become NaN there); the limit of the formula
+  // is used instead, and a unit square around a single point
+  if (w == 0 && h == 0) {
+    xmin -= 0.5;
+    xmax += 0.5;
+    ymin -= 0.5;
+    ymax += 0.5;
+  } else if (w > h) {
     double c = (ymin + ymax) / 2;
-    ymin = w * (ymin - c) / h + c;
-    ymax = w * (ymax - c) / h + c;
+    if (h > 0) {
+      ymin = w * (ymin - c) / h + c;
+      ymax = w * (ymax - c) / h + c;
+    } else {
+      ymin = c - w / 2;
+      ymax = c + w / 2;
+    }
   } else {
     double c = (xmin + xmax) / 2;
-    xmin = h * (xmin - c) / w + c;
-    xmax = h * (xmax - c) / w + c;
+    if (w > 0) {
+      xmin = h * (xmin - c) / w + c;
+      xmax = h * (xmax - c) / w + c;
+    } else {
+      xmin = c - h / 2;
+      xmax = c + h / 2;
+    }
   }
   QNode root;
   root.xmin = xmin; root.ymin = ymin; root.xmax = xmax; root.ymax = ymax;
@@ -176,12 +194,24 @@ class Planner {
  public:
   Planner(Plan &plan, PlanParams const &prm) : P(plan), prm(prm) {}
 
-  int32_t run() {
-    auto sl = P.src.levelsBelow(0);
-    auto tl = P.tgt.levelsBelow(0);
-    auto const &srcNodes = sl[std::min<size_t>(2, sl.size() - 1)];
-    auto const &tgtNodes = tl[std::min<size_t>(2, tl.size() - 1)];
-    return rec(srcNodes, tgtNodes);
+  // bfFacHelm2MakeMultilevel (fac_helm2.c:943-1002) starts from the nodes at
+  // depth 2; a leaf shallower than that (tiny point sets) would leave its
+  // points out of every block, so it joins the list in tree order (for trees
+  // whose depth-1 nodes are all split this is the reference's list)
+  int32_t run() { return rec(frontier(P.src), frontier(P.tgt)); }
+
+  static std::vector<int> frontier(Quadtree const &t) {
+    std::vector<int> out;
+    auto walk = [&](auto &&self, int nd) -> void {
+      std::vector<int> kids = t.children(nd);
+      if (t.nodes[nd].depth == 2 || kids.empty()) {
+        out.push_back(nd);
+        return;
+      }
+      for (int ch : kids) self(self, ch);
+    };
+    for (int ch : t.children(0)) walk(walk, ch);
+    return out;
   }
 
  private:

@@ -225,12 +225,23 @@ class Quadtree:
         xmin, xmax = min(px), max(px)
         ymin, ymax = min(py), max(py)
         w, h = xmax - xmin, ymax - ymin
-        if w > h:
+        # bfBbox2RescaleToSquare (bbox.c:18-30) divides by a zero side for one
+        # point or collinear points; there the limit of its formula (or, for a
+        # single point, a unit square) is used instead
+        if w == 0 and h == 0:
+            xmin, xmax, ymin, ymax = xmin - 0.5, xmax + 0.5, ymin - 0.5, ymax + 0.5
+        elif w > h:
             c = (ymin + ymax) / 2
-            ymin, ymax = w * (ymin - c) / h + c, w * (ymax - c) / h + c
+            if h > 0:
+                ymin, ymax = w * (ymin - c) / h + c, w * (ymax - c) / h + c
+            else:
+                ymin, ymax = c - w / 2, c + w / 2
         else:
             c = (xmin + xmax) / 2
-            xmin, xmax = h * (xmin - c) / w + c, h * (xmax - c) / w + c
+            if w > 0:
+                xmin, xmax = h * (xmin - c) / w + c, h * (xmax - c) / w + c
+            else:
+                xmin, xmax = c - h / 2, c + h / 2
         self.root = QNode((xmin, ymin, xmax, ymax), 0, None, None)
         self.leaf_size = leaf_size
         self._build(self.root, px, py, 0, n)
@@ -379,13 +390,27 @@ class Planner:
         self.eps = eps
         self.leaf_guard = leaf_guard
 
-    # bfFacHelm2MakeMultilevel (fac_helm2.c:943-1002)
+    # bfFacHelm2MakeMultilevel (fac_helm2.c:943-1002) starts from the nodes
+    # at depth 2; a leaf shallower than that (tiny point sets) would leave its
+    # points out of every block, so it joins the list in tree order (for
+    # trees whose depth-1 nodes are all split this is the reference's list)
+    @staticmethod
+    def _frontier(tree):
+        out = []
+
+        def walk(nd):
+            kids = nd.children()
+            if nd.depth == 2 or not kids:
+                out.append(nd)
+            else:
+                for ch in kids:
+                    walk(ch)
+        for ch in tree.root.children():
+            walk(ch)
+        return out
+
     def plan(self):
-        src_levels = self.src.levels_below(self.src.root)
-        tgt_levels = self.tgt.levels_below(self.tgt.root)
-        sl = src_levels[min(2, len(src_levels) - 1)]
-        tl = tgt_levels[min(2, len(tgt_levels) - 1)]
-        return self._rec(sl, tl)
+        return self._rec(self._frontier(self.src), self._frontier(self.tgt))
 
     # facHelm2MakeMultilevel_rec (fac_helm2.c:860-941)
     def _rec(self, src_nodes, tgt_nodes):
