@@ -26,7 +26,10 @@
 namespace bfg {
 namespace {
 
-constexpr int kTcStages = 3;
+// even: stage s then only ever holds chunks of one parity, so each stage's
+// barriers are waited on by one MMA thread, in order (an mbarrier parity wait
+// must not run more than one phase ahead of the barrier)
+constexpr int kTcStages = 4;
 constexpr int kTcRhs = 16;                 // RHS per CTA
 constexpr int kTcN = 2 * kTcRhs;           // MMA N: real and imaginary columns
 constexpr int kAPlaneBytes = 64 * 128;     // at most 64 core matrices per plane
@@ -34,7 +37,8 @@ constexpr int kBPlaneBytes = (kTcChunkCols / 4) * (kTcN / 8) * 128;      // 8 KB
 constexpr int kBuilders = 128;             // warps 0-3: B planes
 constexpr int kExtractors = 128;           // warps 4-7: TMEM partial sums and stores
 constexpr int kProducerWarp = (kBuilders + kExtractors) / 32, kMmaWarp = kProducerWarp + 1;
-constexpr int kTcThreads = kBuilders + kExtractors + 64;   // + bulk-copy warp + MMA warp
+// + one bulk-copy warp + two MMA warps (even / odd chunks)
+constexpr int kTcThreads = kBuilders + kExtractors + 96;
 constexpr uint64_t kWaitLimitNs = 1000000000ull;                          // 1 s
 
 constexpr int kXStageBytes = kTcChunkCols * kTcRhs * 8;                   // 8 KB
@@ -55,6 +59,8 @@ struct TcLayout {
   static constexpr int barOff = kTcStages * stageBytes + 2048;
   // fullA[S], fullB[S], empty[S], accFull[2], accEmpty[2], TMEM slot, abort
   static constexpr int smemBytes = barOff + 8 * (3 * kTcStages + 4) + 16;
+  static_assert(smemBytes <= 232448, "shared memory per CTA");
+  static_assert(kTcStages % 2 == 0, "stages must hold one chunk parity each");
 };
 
 // instruction descriptor: D f32, A and B bf16, both K-major, M = 128, N = n.
@@ -243,12 +249,13 @@ __global__ void __launch_bounds__(256) tcFillKernel(TcFill const *__restrict__ f
 
 // Persistent CTA over its chunk stream (one apply stage, one tile of 16 RHS),
 // warp-specialised around mbarriers:
-//   warp 8 (lane 0)  bulk-copies the A planes of chunk i into stage i % 3
-//                    once the MMAs of chunk i-3 are done (empty);
+//   warp 8 (lane 0)  bulk-copies the A planes of chunk i into stage i % 4
+//                    once the MMAs of chunk i-4 are done (empty);
 //   warps 0-3        copy chunk i+2's FP32 right-hand sides into its stage
 //                    (cp.async) and build chunk i's bf16 B planes (fullB);
-//   warp 9 (lane 0)  issues chunk i's MMAs into TMEM buffer i % 2 once its A
-//                    and B planes have landed and the buffer was read;
+//   warps 9, 10      (lane 0) issue the MMAs of the even and the odd chunks,
+//                    chunk i into TMEM buffer i % 2, once its A and B planes
+//                    have landed and the buffer was read;
 //   warps 4-7        read each chunk's partial sums from TMEM (accFull) into
 //                    FP32 registers, release the buffer (accEmpty) and store
 //                    finished items.
@@ -333,18 +340,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
         for (int64_t j = issued > S ? issued - S : 0; j < issued; ++j)
           mbarDrain(fullA + 8 * (j % S), (uint32_t)((j / S) & 1));
     }
-  } else if (warp == kMmaWarp) {
-    // ---- MMAs ----
-    if (lane == 0) {
+  } else if (warp == kMmaWarp || warp == kMmaWarp + 1) {
+    // ---- MMAs: warp kMmaWarp issues the even chunks, the next warp the odd
+    // ones, so one thread's waits and bookkeeping overlap the other's MMAs in
+    // the tensor pipe; chunk i uses TMEM buffer i % 2, i.e. its thread's own ----
+    int const parity = warp - kMmaWarp;
+    if (lane == 0 && parity < nCh) {
       int64_t last = -1;
-      int32_t kg = ch[0].kg, mg = ch[0].mg;
-      for (int64_t i = 0; i < nCh; ++i) {
+      int32_t kg = ch[parity].kg, mg = ch[parity].mg;
+      for (int64_t i = parity; i < nCh; i += 2) {
         int const s = (int)(i % S), b = (int)(i & 1);
         uint32_t const ph = (uint32_t)((i / S) & 1);
         int32_t kgN = 0, mgN = 0;
-        if (i + 1 < nCh) {
-          kgN = ch[i + 1].kg;
-          mgN = ch[i + 1].mg;
+        if (i + 2 < nCh) {
+          kgN = ch[i + 2].kg;
+          mgN = ch[i + 2].mg;
         }
         if (!mbarWait(fullA + 8 * s, ph, abortFlag) || !mbarWait(fullB + 8 * s, ph, abortFlag) ||
             (i >= 2 && !mbarWait(accEmpty + 8 * b, (uint32_t)(((i >> 1) - 1) & 1), abortFlag))) {
@@ -437,7 +447,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
         int const s = (int)(i % S);
         Cd const d3 = loadCd(i + 3);   // used from the next iteration on
         // inputs of chunk i+2 into its stage: that stage's X area last held
-        // chunk i-1, which this thread has converted
+        // chunk i+2-S, which this thread has converted
         if (i + 2 < nCh) issueX(d2, i + 2);
         cpAsyncCommit();
         if (i >= S && !mbarWait(empty + 8 * s, (uint32_t)((i / S - 1) & 1), abortFlag)) {
