@@ -63,13 +63,15 @@ struct TcLayout {
   static_assert(kTcStages % 2 == 0, "stages must hold one chunk parity each");
 };
 
-// instruction descriptor: D f32, A and B bf16, both K-major, M = 128, N = n.
-// D row r lands in TMEM lane r.  (An MMA costs at least ~44 cycles whatever
-// its size and M = 64 runs at half the rate of M = 128, so every chunk uses
-// M = 128 and as wide an N as the planes allow.)
-__host__ __device__ constexpr uint32_t idescN(int n) {
+// instruction descriptor: D f32, A and B bf16, both K-major, M = m, N = n.
+// D row r lands in TMEM lane r for M = 128, and in lane 32 (r / 16) + r % 16
+// for M = 64 (16 rows in each warp's lane quarter).  An MMA costs at least
+// ~44 cycles whatever its size and M = 64 takes as long as M = 128, but it
+// reads half the A bytes from shared memory, which bounds this kernel: items
+// of at most 64 rows use M = 64.
+__host__ __device__ constexpr uint32_t idesc(int m, int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
-         ((uint32_t)(kTcRows >> 4) << 24);
+         ((uint32_t)(m >> 4) << 24);
 }
 
 __device__ __forceinline__ uint32_t smemAddr(void const *p) {
@@ -365,6 +367,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
         uint32_t const aS = sbase + s * L::stageBytes, bS = aS + L::aBytes;
         uint32_t const lboA = (uint32_t)mg * 128;
         int const ksteps = (kg + 1) >> 1;
+        int const mRows = mg <= 8 ? 64 : 128;
         // A plane t times the B planes 0 .. TERMS-1-t, side by side in N: D
         // columns 32 u .. 32 u + 31 collect the products with B plane u.  The
         // descriptors of k-step st are those of k-step 0 with the start
@@ -381,7 +384,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
           uint32_t const dc = d + 256 * (st & 1);   // even / odd k-step chain
 #pragma unroll
           for (int t = 0; t < TERMS; ++t) {
-            tcMma(dc, da[t], db, idescN(kTcN * (TERMS - t)), (st >= 2 || t > 0) ? 1u : 0u);
+            tcMma(dc, da[t], db, idesc(mRows, kTcN * (TERMS - t)), (st >= 2 || t > 0) ? 1u : 0u);
             da[t] += stepA;
           }
           db += stepB;
@@ -533,7 +536,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
         __syncwarp();
         if (lane == 0) mbarArrive(accEmpty + 8 * b);
         if (d.flags & kTcLast) {
-          int const row = e * 32 + lane;
+          // M = 64 chunks (items of <= 64 rows): lanes 16..31 hold no row
+          int const row = d.rows <= 64 ? (lane < 16 ? e * 16 + lane : kTcRows) : e * 32 + lane;
           if (row < d.rows) {
             float2 *out = W + (d.outRow + row) * R + r0;
 #pragma unroll
