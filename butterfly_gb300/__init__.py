@@ -420,6 +420,9 @@ class Fac:
 
     def apply_device(self, x_ptr: int, ldx: int, R: int, y_ptr: int, ldy: int,
                      precision: str = "fp64", original_order: bool = False):
+        """Y = A X on raw device pointers (bfgFacApply), on the context's
+        stream -- not torch's: order it against torch work with
+        ``ctx.on_stream``.  Applies of one factorization share its workspace."""
         flags = APPLY_ORIGINAL_ORDER if original_order else 0
         self.ctx.check(lib().bfgFacApply(self.handle, PRECISIONS[precision], _VP(x_ptr), ldx, R,
                                          _VP(y_ptr), ldy, flags), "apply")

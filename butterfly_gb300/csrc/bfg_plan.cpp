@@ -862,8 +862,14 @@ void makeTcSchedule(ApplyProgram const &prog, int terms, int ctas, TcSchedule &s
           sc.fills.push_back(f);
           arena += (int64_t)terms * k.kg * mg * 128;
           ch.push_back(k);
-          // a chunk costs its tile bytes plus a fixed handshake
-          cost[(size_t)(i - a)] += (int64_t)k.kg * mg + 8;
+          // time of a chunk on the tensor-core kernel, in units of ~10 ns: a
+          // fixed hand-off (~0.6 us) plus TERMS MMAs per k-step, or its tile
+          // bytes at the CTA's share of HBM bandwidth if that is longer
+          // (per-CTA durations measured on the GB300 follow the chunk count,
+          // not the bytes)
+          int64_t const ksteps = (k.kg + 1) / 2;
+          cost[(size_t)(i - a)] += std::max<int64_t>(
+              60 + terms * ksteps, (int64_t)k.kg * mg * terms * 29 / 100);
         }
       }
       // every block has at least one column, so every item has a chunk

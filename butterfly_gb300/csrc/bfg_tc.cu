@@ -42,6 +42,7 @@ constexpr int kTcThreads = kBuilders + kExtractors + 96;
 constexpr uint64_t kWaitLimitNs = 1000000000ull;                          // 1 s
 
 constexpr int kXStageBytes = kTcChunkCols * kTcRhs * 8;                   // 8 KB
+constexpr int32_t kTcBulkX = 1, kTcBulkW = 2;   // inputs / intermediates by bulk copy
 
 template <int TERMS>
 struct TcLayout {
@@ -251,10 +252,12 @@ __global__ void __launch_bounds__(256) tcFillKernel(TcFill const *__restrict__ f
 
 // Persistent CTA over its chunk stream (one apply stage, one tile of 16 RHS),
 // warp-specialised around mbarriers:
-//   warp 8 (lane 0)  bulk-copies the A planes of chunk i into stage i % 4
-//                    once the MMAs of chunk i-4 are done (empty);
-//   warps 0-3        copy chunk i+2's FP32 right-hand sides into its stage
-//                    (cp.async) and build chunk i's bf16 B planes (fullB);
+//   warp 8           bulk-copies the A planes of chunk i into stage i % 4
+//                    once the MMAs of chunk i-4 are done (empty), and with
+//                    them (fullA) the chunk's FP32 right-hand-side rows when
+//                    they form one aligned block;
+//   warps 0-3        otherwise copy chunk i+2's right-hand sides into its
+//                    stage (cp.async); build chunk i's bf16 B planes (fullB);
 //   warps 9, 10      (lane 0) issue the MMAs of the even and the odd chunks,
 //                    chunk i into TMEM buffer i % 2, once its A and B planes
 //                    have landed and the buffer was read;
@@ -272,7 +275,7 @@ template <int TERMS>
 __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
     TcChunk const *__restrict__ chunks, int64_t const *__restrict__ ctaChunk0,
     uint8_t const *__restrict__ tarena, float2 const *__restrict__ X, int64_t ldx,
-    float2 *__restrict__ W, int64_t R, int32_t *status) {
+    float2 *__restrict__ W, int64_t R, int32_t xBulk, int32_t *status) {
   using L = TcLayout<TERMS>;
   constexpr int S = kTcStages;
   constexpr int kBKGroupBytes = L::kBKGroupBytes;
@@ -284,6 +287,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
   int64_t const r0 = (int64_t)blockIdx.y * kTcRhs;
   int const nr = (R - r0) < kTcRhs ? (int)(R - r0) : kTcRhs;
   TcChunk const *ch = chunks + c0;
+  // a chunk's right-hand sides arrive by one bulk copy with its A planes when
+  // they form a contiguous 16-byte aligned block (16 RHS, leading dimension
+  // 16), else by the builders' cp.async (one copy per 128 B row was slower:
+  // the copy engine takes small copies one at a time)
+  bool const bulkX = nr == kTcRhs && (xBulk & kTcBulkX);
+  bool const bulkW = nr == kTcRhs && (xBulk & kTcBulkW);
 
   uint32_t const sbase = smemAddr(smem);
   uint32_t const fullA = sbase + L::barOff, fullB = fullA + 8 * S, empty = fullB + 8 * S;
@@ -311,37 +320,54 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
   uint32_t const tmem = *tmemSlot;
 
   if (warp == kProducerWarp) {
-    // ---- bulk copies of the A planes ----
-    if (lane == 0) {
-      int64_t issued = 0;
-      // descriptors are read one chunk ahead, off the wait-issue path
-      int64_t off = ch[0].tileOff;
-      uint32_t plane = (uint32_t)ch[0].kg * ch[0].mg * 128;
-      for (int64_t i = 0; i < nCh; ++i) {
-        int const s = (int)(i % S);
-        int64_t offN = 0;
-        uint32_t planeN = 0;
-        if (i + 1 < nCh) {
-          offN = ch[i + 1].tileOff;
-          planeN = (uint32_t)ch[i + 1].kg * ch[i + 1].mg * 128;
-        }
-        if (i >= S && !mbarWait(empty + 8 * s, (uint32_t)((i / S - 1) & 1), abortFlag)) {
-          *abortFlag = 1;
-          break;
-        }
-        mbarExpectTx(fullA + 8 * s, plane * TERMS);
+    // ---- bulk copies of the A planes and of the input rows (lane 0) ----
+    int64_t issued = 0;
+    // descriptors are read one chunk ahead, off the wait-issue path
+    TcChunk const *cp = ch;
+    int64_t off = cp->tileOff, inRow = cp->inRow;
+    uint32_t plane = (uint32_t)cp->kg * cp->mg * 128;
+    int32_t nc = cp->nc, inIsX = cp->inIsX;
+    for (int64_t i = 0; i < nCh; ++i) {
+      int const s = (int)(i % S);
+      int64_t offN = 0, inRowN = 0;
+      uint32_t planeN = 0;
+      int32_t ncN = 0, inIsXN = 0;
+      if (i + 1 < nCh) {
+        offN = ch[i + 1].tileOff;
+        inRowN = ch[i + 1].inRow;
+        planeN = (uint32_t)ch[i + 1].kg * ch[i + 1].mg * 128;
+        ncN = ch[i + 1].nc;
+        inIsXN = ch[i + 1].inIsX;
+      }
+      int ok = 1;
+      if (i >= S && lane == 0) ok = mbarWait(empty + 8 * s, (uint32_t)((i / S - 1) & 1), abortFlag);
+      if (!__shfl_sync(0xffffffffu, ok, 0)) {
+        if (lane == 0) *abortFlag = 1;
+        break;
+      }
+      bool const bulk = inIsX ? bulkX : bulkW;
+      if (lane == 0) {
+        mbarExpectTx(fullA + 8 * s, plane * TERMS + (bulk ? (uint32_t)nc * 128 : 0u));
 #pragma unroll
         for (int t = 0; t < TERMS; ++t)
           bulkG2S(sbase + s * L::stageBytes + t * kAPlaneBytes, tarena + off + (int64_t)t * plane,
                   plane, fullA + 8 * s);
-        issued = i + 1;
-        off = offN;
-        plane = planeN;
       }
-      if (*abortFlag)   // copies still in flight land before the CTA exits
-        for (int64_t j = issued > S ? issued - S : 0; j < issued; ++j)
-          mbarDrain(fullA + 8 * (j % S), (uint32_t)((j / S) & 1));
+      __syncwarp();
+      // the chunk's input rows are one contiguous block (leading dimension 16)
+      if (bulk && lane == 0)
+        bulkG2S(sbase + s * L::stageBytes + L::aBytes + L::bBytes,
+                (inIsX ? X : W) + inRow * kTcRhs, (uint32_t)nc * (kTcRhs * 8), fullA + 8 * s);
+      issued = i + 1;
+      off = offN;
+      inRow = inRowN;
+      plane = planeN;
+      nc = ncN;
+      inIsX = inIsXN;
     }
+    if (lane == 0 && *abortFlag)   // copies still in flight land before the CTA exits
+      for (int64_t j = issued > S ? issued - S : 0; j < issued; ++j)
+        mbarDrain(fullA + 8 * (j % S), (uint32_t)((j / S) & 1));
   } else if (warp == kMmaWarp || warp == kMmaWarp + 1) {
     // ---- MMAs: warp kMmaWarp issues the even chunks, the next warp the odd
     // ones, so one thread's waits and bookkeeping overlap the other's MMAs in
@@ -425,34 +451,48 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
     };
     if (tid < kBuilders) {
       // ---- B planes ----
-      // Element (j, q) of a k-step's 8 columns x 16 RHS belongs to one
-      // builder: j = 8 st + (lane & 3) + 4 (warp & 1), q = (lane >> 2) +
-      // 8 (warp >> 1), so a warp's B stores fall in 32 distinct banks.  The
-      // thread that copies an element into the X stage is the one that
-      // converts it, so the cp.async groups need no barrier.  Descriptors are
-      // loaded one iteration before their first use.
-      int const jOff = (lane & 3) + 4 * (warp & 1), q = (lane >> 2) + 8 * (warp >> 1);
+      // A builder converts columns j0 .. j0+3 (j0 = 4 jg: one k-group) of RHS
+      // q, jg = (lane >> 4) + 2 warp + 8 p for passes p = 0, 1: the four
+      // complex values fill one 16 B core-matrix row of each B plane, and a
+      // warp's stores cover 512 contiguous-in-banks bytes.  On the cp.async
+      // path the thread that copies an element into the X stage is the one
+      // that converts it, so the cp.async groups need no barrier.
+      // Descriptors are loaded one iteration before their first use.
+      int const q = lane & 15, jgBase = (lane >> 4) + 2 * warp;
       auto issueX = [&](Cd const &d, int64_t i) {
         int64_t const xld = d.inIsX ? ldx : R;
         float2 const *src = (d.inIsX ? X : W) + d.inRow * xld + r0 + q;
         uint32_t const xs = sbase + (int)(i % S) * L::stageBytes + L::aBytes + L::bBytes;
         if (q < nr)
-          for (int j = jOff; j < d.nc; j += 8)
-            cpAsync8(xs + (uint32_t)(j * kTcRhs + q) * 8, src + (int64_t)j * xld);
+#pragma unroll
+          for (int p = 0; p < 2; ++p)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              int const j = 4 * (jgBase + 8 * p) + u;
+              if (j < d.nc) cpAsync8(xs + (uint32_t)(j * kTcRhs + q) * 8, src + (int64_t)j * xld);
+            }
       };
+      auto bulkOf = [&](Cd const &d) { return d.inIsX ? bulkX : bulkW; };
       Cd d0 = loadCd(0), d1 = loadCd(1), d2 = loadCd(2);
       // inputs of chunks 0 and 1 in flight before the loop (two cp.async groups)
-      if (0 < nCh) issueX(d0, 0);
+      if (0 < nCh && !bulkOf(d0)) issueX(d0, 0);
       cpAsyncCommit();
-      if (1 < nCh) issueX(d1, 1);
+      if (1 < nCh && !bulkOf(d1)) issueX(d1, 1);
       cpAsyncCommit();
       for (int64_t i = 0; i < nCh; ++i) {
         int const s = (int)(i % S);
         Cd const d3 = loadCd(i + 3);   // used from the next iteration on
         // inputs of chunk i+2 into its stage: that stage's X area last held
         // chunk i+2-S, which this thread has converted
-        if (i + 2 < nCh) issueX(d2, i + 2);
+        if (i + 2 < nCh && !bulkOf(d2)) issueX(d2, i + 2);
         cpAsyncCommit();
+        // bulk inputs land with the A planes, which the producer copies only
+        // once the MMAs of chunk i-S are done; the empty wait then returns
+        // at once
+        if (bulkOf(d0) && !mbarWait(fullA + 8 * s, (uint32_t)((i / S) & 1), abortFlag)) {
+          *abortFlag = 1;
+          break;
+        }
         if (i >= S && !mbarWait(empty + 8 * s, (uint32_t)((i / S - 1) & 1), abortFlag)) {
           *abortFlag = 1;
           break;
@@ -461,22 +501,32 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
         uint8_t *stage = smem + s * L::stageBytes;
         uint8_t *bsm = stage + L::aBytes;
         float2 const *xs = reinterpret_cast<float2 const *>(stage + L::aBytes + L::bBytes);
-        int const ksteps = (d0.kg + 1) >> 1;
-        for (int st = 0; st < ksteps; ++st) {
-          int const j = 8 * st + jOff;
-          float2 const v = (j < d0.nc && q < nr) ? xs[j * kTcRhs + q] : make_float2(0.f, 0.f);
-          uint32_t pr[TERMS];
-          splitPair<TERMS>(v.x, v.y, pr);
-          int const kk = 2 * j;
-          uint32_t const offRe =
-              (kk >> 3) * kBKGroupBytes + (q >> 3) * 128 + (q & 7) * 16 + (kk & 7) * 2;
-          uint32_t const offIm = offRe + 2 * 128;   // column 16 + q: two core rows further
+        int const kgEven = ((d0.kg + 1) >> 1) * 2;   // k-groups the MMAs read
 #pragma unroll
-          for (int t = 0; t < TERMS; ++t) {
-            // rows 2j, 2j+1 of column q: (Re x, -Im x); of column 16+q: (Im x, Re x)
-            *reinterpret_cast<uint32_t *>(bsm + t * 512 + offRe) = pr[t] ^ 0x80000000u;
-            *reinterpret_cast<uint32_t *>(bsm + t * 512 + offIm) =
-                __byte_perm(pr[t], 0, 0x1032);
+        for (int p = 0; p < 2; ++p) {
+          int const jg = jgBase + 8 * p;
+          if (jg < kgEven) {
+            float2 v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              int const j = 4 * jg + u;
+              v[u] = (j < d0.nc && q < nr) ? xs[j * kTcRhs + q] : make_float2(0.f, 0.f);
+            }
+            uint32_t pr[4][TERMS];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) splitPair<TERMS>(v[u].x, v[u].y, pr[u]);
+            uint32_t const offRe = (uint32_t)jg * kBKGroupBytes + (q >> 3) * 128 + (q & 7) * 16;
+#pragma unroll
+            for (int t = 0; t < TERMS; ++t) {
+              // rows 2j, 2j+1 of column q: (Re x, -Im x); of column 16+q
+              // (two core rows further): (Im x, Re x)
+              *reinterpret_cast<uint4 *>(bsm + t * 512 + offRe) =
+                  make_uint4(pr[0][t] ^ 0x80000000u, pr[1][t] ^ 0x80000000u,
+                             pr[2][t] ^ 0x80000000u, pr[3][t] ^ 0x80000000u);
+              *reinterpret_cast<uint4 *>(bsm + t * 512 + offRe + 2 * 128) =
+                  make_uint4(__byte_perm(pr[0][t], 0, 0x1032), __byte_perm(pr[1][t], 0, 0x1032),
+                             __byte_perm(pr[2][t], 0, 0x1032), __byte_perm(pr[3][t], 0, 0x1032));
+            }
           }
         }
         // an odd k-group count leaves the second half of the last k-step unset
@@ -604,12 +654,15 @@ cudaError_t launchApplyTc(int32_t terms, TcChunk const *chunks, int64_t const *c
                           float2 *W, int64_t R, int32_t *status, cudaStream_t stream) {
   if (ctas == 0) return cudaSuccess;
   dim3 grid((unsigned)ctas, (unsigned)((R + kTcRhs - 1) / kTcRhs));
+  // one bulk copy per chunk: 16 RHS with leading dimension 16, 16-byte aligned
+  int32_t const xBulk = ((R == kTcRhs && ldx == kTcRhs && (uintptr_t)X % 16 == 0) ? kTcBulkX : 0) |
+                        ((R == kTcRhs && (uintptr_t)W % 16 == 0) ? kTcBulkW : 0);
   if (terms == 3)
     applyTcKernel<3><<<grid, kTcThreads, TcLayout<3>::smemBytes, stream>>>(chunks, ctaChunk0, tarena, X,
-                                                                     ldx, W, R, status);
+                                                                     ldx, W, R, xBulk, status);
   else
     applyTcKernel<2><<<grid, kTcThreads, TcLayout<2>::smemBytes, stream>>>(chunks, ctaChunk0, tarena, X,
-                                                                     ldx, W, R, status);
+                                                                     ldx, W, R, xBulk, status);
   return cudaGetLastError();
 }
 

@@ -180,7 +180,9 @@ bfgStatus bfgFacCopyBlocks(bfgFac fac, double *entries, int64_t capacityEntries,
  * precision other than FP64 builds that precision's copy of the factors
  * (allocates and synchronises once).  Rows are in tree order unless
  * BFG_APPLY_ORIGINAL_ORDER is set.  Runs on the context's stream; returns
- * without synchronising. */
+ * without synchronising.  Every apply of one factorization uses its one
+ * workspace: applies issued on different streams must be ordered by the
+ * caller (events), as must the writes of X and reads of Y on other streams. */
 bfgStatus bfgFacApply(bfgFac fac, bfgPrecision precision, void const *X, int64_t ldx,
                       int64_t numRhs, void *Y, int64_t ldy, uint32_t flags);
 

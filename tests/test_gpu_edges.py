@@ -61,7 +61,10 @@ def test_single_rhs_and_strided_operands_every_precision(ctx, prec):
     # one column, taken from a 4-column matrix (leading dimension 4)
     Xs = X.to(dt)
     Y = torch.zeros((n, 3), dtype=dt, device="cuda")      # leading dimension 3
-    fac.apply_device(Xs[:, 1:].data_ptr(), 4, 1, Y.data_ptr(), 3, prec)
+    # the raw-pointer call runs on the context's stream: put it on torch's,
+    # behind the fill of Y and the applies above (they share the workspace)
+    with fac.ctx.on_stream(torch.cuda.current_stream().cuda_stream):
+        fac.apply_device(Xs[:, 1:].data_ptr(), 4, 1, Y.data_ptr(), 3, prec)
     torch.cuda.synchronize()
     y = Y[:, 0].cpu().numpy().astype(np.complex128)
     assert rel_err(y, y64[:, 1].cpu().numpy()) < tol
