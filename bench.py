@@ -58,7 +58,7 @@ METRIC = "Butterfly apply RHS/s at 1e-6 rel err vs plain FP64 GPU; GMRES time-to
 # reports its dominant launch's traffic as this ratio times its own
 # algorithmic bytes
 NCU_DRAM_PER_ALG = {("fp32", 16, 5): [0.7973, 1.0266, 0.9855, 0.7925],
-                    ("bf16x3", 16, 5): [0.8870, 1.0633, 1.0222, 0.9028]}
+                    ("bf16x3", 16, 5): [0.8888, 1.0627, 1.0246, 1.0386]}
 ERR_BOUND = 1e-6
 
 
@@ -556,7 +556,8 @@ def main():
     dom = int(np.argmax(per))
     sA = {"fp64": 16, "fp32": 8, "bf16x3": 12, "bf16x2": 8}[head]
     sv = 16 if head == "fp64" else 8
-    alg_bytes = float(info[dom, 0] * sA + R * sv * (info[dom, 1] + info[dom, 2]))
+    alg_all = [float(e * sA + R * sv * (ri + ro)) for e, ri, ro in info]
+    alg_bytes = alg_all[dom]
     launch_share = [float(v) for v in per / per.sum()]
     peaks = {}
     try:
@@ -576,7 +577,7 @@ def main():
             "peak_source": peak_src,
             "kernel": "apply launch %d of %d" % (dom, len(per)),
             "launch_ms": float(per[dom]), "alg_bytes": alg_bytes,
-            "launch_share": launch_share,
+            "launch_share": launch_share, "alg_bytes_per_launch": alg_all,
             "flops_per_s": float(8.0 * info[dom, 0] * R / (per[dom] / 1e3))}
 
     # end to end through the C ABI with pinned host complex128 operands

@@ -21,6 +21,7 @@
 #include <cstdio>
 #include <map>
 #include <stdexcept>
+#include <tuple>
 
 namespace bfg {
 
@@ -675,14 +676,13 @@ void makeApplyProgram(Plan const &plan, ApplyProgram &prog, int itemRows) {
   int64_t ws = 0;
   double flops = 0;
 
+  // merge (optional): output row -> item of this stage already writing it;
+  // a block row whose items exist adds its blocks to them
   auto addBlockRows = [&](size_t stage, int64_t outBase, int64_t rows,
                           std::vector<std::pair<Block const *, int64_t>> const &blks,
-                          int inIsX) {
+                          int inIsX, std::map<int64_t, size_t> *merge) {
     // blks: (block, first input row); all share the block row
     for (int64_t r0 = 0; r0 < rows; r0 += itemRows) {
-      ApplyItem it{};
-      it.outRow = outBase + r0;
-      it.rows = (int32_t)std::min<int64_t>(itemRows, rows - r0);
       std::vector<ApplyContrib> cs;
       for (auto const &bp : blks) {
         ApplyContrib c{};
@@ -693,12 +693,39 @@ void makeApplyProgram(Plan const &plan, ApplyProgram &prog, int itemRows) {
         c.inIsX = inIsX;
         cs.push_back(c);
       }
-      it.nContrib = (int32_t)cs.size();
       stageFor(stage);
+      int64_t const outRow = outBase + r0;
+      if (merge) {
+        auto hit = merge->find(outRow);
+        if (hit != merge->end()) {
+          auto &dst = stContribs[stage][hit->second];
+          dst.insert(dst.end(), cs.begin(), cs.end());
+          stItems[stage][hit->second].nContrib = (int32_t)dst.size();
+          continue;
+        }
+        (*merge)[outRow] = stItems[stage].size();
+      }
+      ApplyItem it{};
+      it.outRow = outRow;
+      it.rows = (int32_t)std::min<int64_t>(itemRows, rows - r0);
+      it.nContrib = (int32_t)cs.size();
       stItems[stage].push_back(it);
       stContribs[stage].push_back(std::move(cs));
     }
   };
+  // Products with the same target rows, factor count and last-factor row
+  // partition (the butterflies of one target box against the source boxes
+  // of the frontier) write their last factor into one region, up to
+  // kFinGroup of them: each item of it accumulates the final blocks of all,
+  // so the stage writes each target row once per group instead of once per
+  // product and the final sum has that many fewer terms.  (Larger groups
+  // make items so long that the tensor-core CTAs balance poorly.)
+  struct FinGroup {
+    int64_t fin;
+    int members;
+    std::map<int64_t, size_t> items;
+  };
+  std::map<std::tuple<int64_t, int64_t, size_t, std::vector<int64_t>>, FinGroup> finGroups;
 
   // walk the HODBF in plan order, assigning workspace regions
   std::vector<std::pair<int32_t, std::pair<int64_t, int64_t>>> st;
@@ -725,7 +752,7 @@ void makeApplyProgram(Plan const &plan, ApplyProgram &prog, int itemRows) {
       Block const &b = plan.blocks[nd.block];
       int64_t base = ws;
       ws += b.m;
-      addBlockRows(0, base, b.m, {{&b, b.s0}}, 1);
+      addBlockRows(0, base, b.m, {{&b, b.s0}}, 1, nullptr);
       regions.push_back({b.t0, b.t1, base});
       flops += 8.0 * b.m * b.n;
       prog.stageEntries[0] += (int64_t)b.m * b.n;
@@ -743,9 +770,18 @@ void makeApplyProgram(Plan const &plan, ApplyProgram &prog, int itemRows) {
     }
     int64_t base = ws;
     ws += 2 * maxMid;
-    int64_t fin = ws;
-    ws += pr.t1 - pr.t0;
-    regions.push_back({pr.t0, pr.t1, fin});
+    Factor const &lastF = plan.factors[pr.factors[0]];
+    auto key = std::make_tuple(pr.t0, pr.t1, nf, lastF.rowOff);
+    auto grp = finGroups.find(key);
+    bool const joined = grp != finGroups.end() && grp->second.members < kFinGroup;
+    if (joined) {
+      ++grp->second.members;
+    } else {
+      grp = finGroups.insert_or_assign(key, FinGroup{ws, 1, {}}).first;
+      ws += pr.t1 - pr.t0;
+      regions.push_back({pr.t0, pr.t1, grp->second.fin});
+    }
+    int64_t const fin = grp->second.fin;
     for (size_t a = 0; a < nf; ++a) {
       Factor const &f = plan.factors[pr.factors[nf - 1 - a]];
       bool first = a == 0, last = a + 1 == nf;
@@ -761,13 +797,13 @@ void makeApplyProgram(Plan const &plan, ApplyProgram &prog, int itemRows) {
       for (int32_t i = 0; i < f.nbr; ++i) {
         if (byRow[i].empty()) continue;
         addBlockRows(a, outBase + f.rowOff[i], f.rowOff[i + 1] - f.rowOff[i], byRow[i],
-                     first ? 1 : 0);
+                     first ? 1 : 0, last ? &grp->second.items : nullptr);
       }
       stageFor(a);
       for (int32_t bi : f.blocks)
         prog.stageEntries[a] += (int64_t)plan.blocks[bi].m * plan.blocks[bi].n;
       prog.stageRowsIn[a] += f.colOff.back();
-      prog.stageRowsOut[a] += f.rowOff.back();
+      if (!(last && joined)) prog.stageRowsOut[a] += f.rowOff.back();
     }
   }
   prog.wsRows = ws;

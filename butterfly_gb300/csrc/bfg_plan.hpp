@@ -134,6 +134,9 @@ void makePlan(Plan &plan, PlanParams const &params, double const *srcXy,
 // One work item of an apply stage: up to kItemRows consecutive output rows of
 // one block row, accumulating over the blocks in that row.
 constexpr int kItemRows = 32;
+// products whose last factors share one output region (and one item per
+// row range) in an apply program
+constexpr int kFinGroup = 8;
 
 struct ApplyItem {
   int64_t outRow;               // first output row in the workspace
