@@ -245,8 +245,10 @@ def run_batched(args, cfg):
     ctx = B.Context(local)
     sizes, problems, ks = batched_problems(B, cfg)
     t0 = time.perf_counter()
+    # every problem's two quadtrees in one GPU pass (the same trees as the
+    # host build)
     fac = B.make_batched(B.Helm2(1.0), problems, ks, leaf_size=cfg["leaf"], rank_eps=cfg["tol"],
-                         pinv_tol=cfg["tol"], context=ctx)
+                         pinv_tol=cfg["tol"], context=ctx, tree_on_gpu=True)
     fac_s = time.perf_counter() - t0
     n = int(sizes.sum())
     R = args.rhs or cfg["R"]

@@ -45,8 +45,22 @@ class _Helm2C(ctypes.Structure):
 
 class _FacOptionsC(ctypes.Structure):
     _fields_ = [("leafSize", ctypes.c_int64), ("rankEps", ctypes.c_double),
-                ("pinvCut", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("pinvCut", ctypes.c_int32), ("treeOnGpu", ctypes.c_int32),
                 ("pinvTol", ctypes.c_double)]
+
+
+class _QuadtreeNodeC(ctypes.Structure):
+    _fields_ = [("xmin", ctypes.c_double), ("ymin", ctypes.c_double),
+                ("xmax", ctypes.c_double), ("ymax", ctypes.c_double),
+                ("splitX", ctypes.c_double), ("splitY", ctypes.c_double),
+                ("i0", ctypes.c_int64), ("i1", ctypes.c_int64),
+                ("parent", ctypes.c_int32), ("depth", ctypes.c_int32),
+                ("child", ctypes.c_int32 * 4)]
+
+
+QUADTREE_NODE_DTYPE = np.dtype([("xmin", "f8"), ("ymin", "f8"), ("xmax", "f8"), ("ymax", "f8"),
+                                ("splitX", "f8"), ("splitY", "f8"), ("i0", "i8"), ("i1", "i8"),
+                                ("parent", "i4"), ("depth", "i4"), ("child", "i4", (4,))])
 
 
 class _FacStatsC(ctypes.Structure):
@@ -108,6 +122,7 @@ def lib() -> ctypes.CDLL:
         "bfgPlanHelm2": [ctypes.c_double, _VP, _I64, _VP, _I64, ctypes.POINTER(_FacOptionsC),
                          _VP, _VP, ctypes.c_char_p, _I64, ctypes.POINTER(_I64)],
         "bfgBessel01Host": [_VP, _I64, _VP],
+        "bfgQuadtreeBuild": [_VP, _VP, _VP, _I64, _I64, ctypes.c_int32, _VP, _VP, _I64, _VP],
         "bfgRngSeed": [ctypes.POINTER(_RngC), ctypes.c_uint64],
         "bfgRngUniform1": [ctypes.POINTER(_RngC)],
         "bfgRngUniform": [ctypes.POINTER(_RngC), _I64, _VP],
@@ -260,6 +275,7 @@ class FacHelm2:
     @staticmethod
     def make_multilevel(helm: Helm2, src_tree: Quadtree, tgt_tree: Quadtree | None = None,
                         *, rank_eps: float = 1e-15, pinv_tol: float | None = None,
+                        tree_on_gpu: bool = False,
                         context: Context | None = None) -> "Fac":
         tgt_tree = src_tree if tgt_tree is None else tgt_tree
         if src_tree.leaf_size != tgt_tree.leaf_size:
@@ -271,6 +287,7 @@ class FacHelm2:
         lib().bfgFacOptionsDefault(ctypes.byref(opts))
         opts.leafSize = int(src_tree.leaf_size)
         opts.rankEps = float(rank_eps)
+        opts.treeOnGpu = 1 if tree_on_gpu else 0
         if pinv_tol is not None:
             opts.pinvCut, opts.pinvTol = 1, float(pinv_tol)
         h = _VP()
@@ -282,7 +299,8 @@ class FacHelm2:
 
 
 def make_batched(helm: Helm2, problems, ks, *, leaf_size: int = 1, rank_eps: float = 1e-15,
-                 pinv_tol: float | None = None, context: Context | None = None) -> "Fac":
+                 pinv_tol: float | None = None, context: Context | None = None,
+                 tree_on_gpu: bool = False) -> "Fac":
     """Factorize many independent problems in one go (bfgFacHelm2MakeBatched).
     ``problems``: list of (src, tgt) or (src, tgt, src_normals, tgt_normals);
     ``ks``: wavenumber per problem.  The result applies diag(A_0, ..., A_P-1);
@@ -305,6 +323,7 @@ def make_batched(helm: Helm2, problems, ks, *, leaf_size: int = 1, rank_eps: flo
     lib().bfgFacOptionsDefault(ctypes.byref(opts))
     opts.leafSize = int(leaf_size)
     opts.rankEps = float(rank_eps)
+    opts.treeOnGpu = 1 if tree_on_gpu else 0
     if pinv_tol is not None:
         opts.pinvCut, opts.pinvTol = 1, float(pinv_tol)
     h = _VP()
@@ -517,6 +536,35 @@ def plan_helm2(k: float, src, tgt, leaf_size: int = 1, rank_eps: float = 1e-15):
     if st != BFG_OK:
         raise BfgError(st, "plan_helm2 failed")
     return sp, tp, buf.value.decode()
+
+
+def quadtree_build(point_sets, leaf_size: int = 1, on_gpu: bool = False,
+                   context: Context | None = None):
+    """bfQuadtreeInit (quadtree.c:80-98) of each (N_t, 2) point set, on the
+    GPU in one pass over all sets (on_gpu) or on the host: a list of
+    (perm, nodes) per set, perm the tree order (indices into the set), nodes
+    a QUADTREE_NODE_DTYPE array numbered as the reference's recursive build
+    creates them."""
+    sets = [_xy(p) for p in point_sets]
+    off = np.zeros(len(sets) + 1, dtype=np.int64)
+    off[1:] = np.cumsum([len(p) for p in sets])
+    xy = np.ascontiguousarray(np.concatenate(sets) if sets else np.zeros((0, 2)))
+    ctx = (context or default_context()) if on_gpu else context
+    h = ctx.handle if ctx is not None else None
+    perm = np.empty(int(off[-1]), dtype=np.int64)
+    noff = np.empty(len(sets) + 1, dtype=np.int64)
+    L = lib()
+    st = L.bfgQuadtreeBuild(h, _ptr(xy), _ptr(off), len(sets), int(leaf_size), int(bool(on_gpu)),
+                            _ptr(perm), None, 0, _ptr(noff))
+    if st != BFG_OK:
+        raise BfgError(st, "quadtree_build: " + (L.bfgGetErrorString(h).decode() if h else "failed"))
+    nodes = np.zeros(int(noff[-1]), dtype=QUADTREE_NODE_DTYPE)
+    st = L.bfgQuadtreeBuild(h, _ptr(xy), _ptr(off), len(sets), int(leaf_size), int(bool(on_gpu)),
+                            _ptr(perm), _ptr(nodes), len(nodes), _ptr(noff))
+    if st != BFG_OK:
+        raise BfgError(st, "quadtree_build: " + (L.bfgGetErrorString(h).decode() if h else "failed"))
+    return [(perm[off[t]:off[t + 1]].copy(), nodes[noff[t]:noff[t + 1]].copy())
+            for t in range(len(sets))]
 
 
 def bessel01_host(x) -> np.ndarray:

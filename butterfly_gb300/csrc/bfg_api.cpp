@@ -105,6 +105,26 @@ bfgStatus fail(bfgContext ctx, bfgStatus st, std::string const &msg) {
   return st;
 }
 
+// the 2 P quadtrees of P problems (source tree of problem p at 2p, target
+// tree at 2p+1) built on the GPU in one pass over all of them
+std::vector<bfg::Quadtree> gpuTrees(cudaStream_t s, double const *srcXy, int64_t const *srcOff,
+                                    double const *tgtXy, int64_t const *tgtOff, int64_t P,
+                                    int64_t leafSize) {
+  std::vector<int64_t> off((size_t)(2 * P + 1), 0);
+  for (int64_t p = 0; p < P; ++p) {
+    off[(size_t)(2 * p + 1)] = off[(size_t)(2 * p)] + (srcOff[p + 1] - srcOff[p]);
+    off[(size_t)(2 * p + 2)] = off[(size_t)(2 * p + 1)] + (tgtOff[p + 1] - tgtOff[p]);
+  }
+  std::vector<double> xy((size_t)(2 * off.back()));
+  for (int64_t p = 0; p < P; ++p) {
+    std::copy(srcXy + 2 * srcOff[p], srcXy + 2 * srcOff[p + 1], xy.begin() + 2 * off[(size_t)(2 * p)]);
+    std::copy(tgtXy + 2 * tgtOff[p], tgtXy + 2 * tgtOff[p + 1], xy.begin() + 2 * off[(size_t)(2 * p + 1)]);
+  }
+  std::vector<bfg::Quadtree> trees;
+  bfg::buildQuadtreesGpu(xy.data(), off.data(), 2 * P, leafSize, s, trees);
+  return trees;
+}
+
 template <typename F>
 bfgStatus guarded(bfgContext ctx, F &&f) {
   try {
@@ -749,7 +769,13 @@ bfgStatus bfgFacHelm2MakeMultilevel(bfgContext ctx, bfgHelm2 const *helm, double
       pp.k = helm->k;
       pp.leafSize = o.leafSize;
       pp.rankEps = o.rankEps;
-      bfg::makePlan(f->plan, pp, srcXy, numSrc, tgtXy, numTgt);
+      if (o.treeOnGpu) {
+        int64_t const so[2] = {0, numSrc}, to[2] = {0, numTgt};
+        auto trees = gpuTrees(ctx->stream, srcXy, so, tgtXy, to, 1, o.leafSize);
+        bfg::makePlan(f->plan, pp, srcXy, numSrc, tgtXy, numTgt, &trees[0], &trees[1]);
+      } else {
+        bfg::makePlan(f->plan, pp, srcXy, numSrc, tgtXy, numTgt);
+      }
       cudaStream_t s = ctx->stream;
       f->srcHasNormals = srcNormals != nullptr;
       f->tgtHasNormals = tgtNormals != nullptr;
@@ -819,7 +845,14 @@ bfgStatus bfgFacHelm2MakeBatched(bfgContext ctx, bfgHelm2 const *helm, double co
       bfg::PlanParams pp;
       pp.leafSize = o.leafSize;
       pp.rankEps = o.rankEps;
-      bfg::makePlanBatched(f->plan, pp, k, srcXy, srcOffsets, tgtXy, tgtOffsets, numProblems);
+      if (o.treeOnGpu) {
+        auto trees = gpuTrees(ctx->stream, srcXy, srcOffsets, tgtXy, tgtOffsets, numProblems,
+                              o.leafSize);
+        bfg::makePlanBatched(f->plan, pp, k, srcXy, srcOffsets, tgtXy, tgtOffsets, numProblems,
+                             &trees);
+      } else {
+        bfg::makePlanBatched(f->plan, pp, k, srcXy, srcOffsets, tgtXy, tgtOffsets, numProblems);
+      }
       cudaStream_t s = ctx->stream;
       f->srcHasNormals = srcNormals != nullptr;
       f->tgtHasNormals = tgtNormals != nullptr;
@@ -944,12 +977,22 @@ bfgStatus bfgFacLoad(bfgContext ctx, char const *path, bfgFac *out) {
       bfg::PlanParams pp;
       pp.leafSize = h.opts.leafSize;
       pp.rankEps = h.opts.rankEps;
+      int64_t const so1[2] = {0, h.nSrc}, to1[2] = {0, h.nTgt};
+      int64_t const *so = h.batched ? f->inSrcOff.data() : so1;
+      int64_t const *to = h.batched ? f->inTgtOff.data() : to1;
+      int64_t const np = h.batched ? h.numProblems : 1;
+      std::vector<bfg::Quadtree> trees;
+      if (h.opts.treeOnGpu)
+        trees = gpuTrees(ctx->stream, f->inSrcXy.data(), so, f->inTgtXy.data(), to, np,
+                         h.opts.leafSize);
       if (h.batched) {
         bfg::makePlanBatched(f->plan, pp, f->inK.data(), f->inSrcXy.data(), f->inSrcOff.data(),
-                             f->inTgtXy.data(), f->inTgtOff.data(), h.numProblems);
+                             f->inTgtXy.data(), f->inTgtOff.data(), h.numProblems,
+                             trees.empty() ? nullptr : &trees);
       } else {
         pp.k = f->inK[0];
-        bfg::makePlan(f->plan, pp, f->inSrcXy.data(), h.nSrc, f->inTgtXy.data(), h.nTgt);
+        bfg::makePlan(f->plan, pp, f->inSrcXy.data(), h.nSrc, f->inTgtXy.data(), h.nTgt,
+                      trees.empty() ? nullptr : &trees[0], trees.empty() ? nullptr : &trees[1]);
       }
       if (f->plan.arenaEntries != h.arenaEntries)
         throw BfgError{BFG_ERROR_INVALID_ARGUMENTS,
@@ -1263,6 +1306,55 @@ bfgStatus bfgPlanHelm2(double k, double const *srcXy, int64_t numSrc, double con
   } catch (std::exception const &) {
     return BFG_ERROR_RUNTIME;
   }
+}
+
+bfgStatus bfgQuadtreeBuild(bfgContext ctx, double const *xy, int64_t const *setOffsets,
+                           int64_t numSets, int64_t leafSize, int32_t onGpu, int64_t *perm,
+                           bfgQuadtreeNode *nodes, int64_t nodeCapacity, int64_t *nodeOffsets) {
+  if (!xy || !setOffsets || numSets < 1 || leafSize < 1 || !perm || !nodeOffsets ||
+      (onGpu && !ctx) || (nodes && nodeCapacity < 0) || setOffsets[0] != 0)
+    return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "quadtree: bad arguments");
+  for (int64_t t = 0; t < numSets; ++t)
+    if (setOffsets[t + 1] < setOffsets[t])
+      return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "quadtree: decreasing set offsets");
+  int64_t const n = setOffsets[numSets];
+  for (int64_t i = 0; i < 2 * n; ++i)
+    if (!std::isfinite(xy[i])) return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "quadtree: non-finite point");
+  return guarded(ctx, [&]() -> bfgStatus {
+    std::vector<bfg::Quadtree> trees;
+    if (onGpu) {
+      bfg::buildQuadtreesGpu(xy, setOffsets, numSets, leafSize, ctx->stream, trees);
+    } else {
+      trees.resize((size_t)numSets);
+      for (int64_t t = 0; t < numSets; ++t)
+        trees[(size_t)t].build(xy + 2 * setOffsets[t], setOffsets[t + 1] - setOffsets[t], leafSize);
+    }
+    nodeOffsets[0] = 0;
+    for (int64_t t = 0; t < numSets; ++t) {
+      nodeOffsets[t + 1] = nodeOffsets[t] + (int64_t)trees[(size_t)t].nodes.size();
+      std::copy(trees[(size_t)t].perm.begin(), trees[(size_t)t].perm.end(), perm + setOffsets[t]);
+    }
+    if (!nodes) return BFG_OK;
+    if (nodeOffsets[numSets] > nodeCapacity)
+      return fail(ctx, BFG_ERROR_OUT_OF_RANGE, "quadtree: node capacity too small");
+    for (int64_t t = 0; t < numSets; ++t)
+      for (size_t i = 0; i < trees[(size_t)t].nodes.size(); ++i) {
+        bfg::QNode const &q = trees[(size_t)t].nodes[i];
+        bfgQuadtreeNode &o = nodes[nodeOffsets[t] + (int64_t)i];
+        o.xmin = q.xmin;
+        o.ymin = q.ymin;
+        o.xmax = q.xmax;
+        o.ymax = q.ymax;
+        o.splitX = q.sx;
+        o.splitY = q.sy;
+        o.i0 = q.i0;
+        o.i1 = q.i1;
+        o.parent = q.parent;
+        o.depth = q.depth;
+        for (int c = 0; c < 4; ++c) o.child[c] = q.child[c];
+      }
+    return BFG_OK;
+  });
 }
 
 bfgStatus bfgBessel01Host(double const *x, int64_t n, double *out) {

@@ -43,8 +43,7 @@ void Quadtree::build(double const *xy, int64_t n, int64_t leafSize_) {
     px[i] = xy[2 * i];
     py[i] = xy[2 * i + 1];
   }
-  // bfPoints2GetBoundingBox (points.c:415-430) + bfBbox2RescaleToSquare
-  // (bbox.c:18-30)
+  // bfPoints2GetBoundingBox (points.c:415-430)
   double xmin = INFINITY, xmax = -INFINITY, ymin = INFINITY, ymax = -INFINITY;
   for (int64_t i = 0; i < n; ++i) {
     xmin = std::fmin(xmin, px[i]);
@@ -52,6 +51,15 @@ void Quadtree::build(double const *xy, int64_t n, int64_t leafSize_) {
     ymin = std::fmin(ymin, py[i]);
     ymax = std::fmax(ymax, py[i]);
   }
+  QNode root = rootNode(xmin, xmax, ymin, ymax);
+  root.i0 = 0;
+  root.i1 = n;
+  nodes.push_back(root);
+  if (n > 0) split(0, px.data(), py.data());
+}
+
+QNode Quadtree::rootNode(double xmin, double xmax, double ymin, double ymax) {
+  // bfBbox2RescaleToSquare (bbox.c:18-30)
   double w = xmax - xmin, h = ymax - ymin;
   // the reference's formula divides by a zero side for one point or for
   // collinear points (its boxes become NaN there); the limit of the formula
@@ -84,10 +92,20 @@ void Quadtree::build(double const *xy, int64_t n, int64_t leafSize_) {
   root.xmin = xmin; root.ymin = ymin; root.xmax = xmax; root.ymax = ymax;
   root.sx = (xmin + xmax) / 2;
   root.sy = (ymin + ymax) / 2;
-  root.i0 = 0;
-  root.i1 = n;
-  nodes.push_back(root);
-  if (n > 0) split(0, px.data(), py.data());
+  return root;
+}
+
+QNode Quadtree::childNode(QNode const &par, int q) {
+  double const xmin = par.xmin, ymin = par.ymin, xmax = par.xmax, ymax = par.ymax;
+  double const sx = par.sx, sy = par.sy;
+  double const box[4][4] = {{xmin, ymin, sx, sy}, {xmin, sy, sx, ymax},
+                            {sx, ymin, xmax, sy}, {sx, sy, xmax, ymax}};
+  QNode ch;
+  ch.xmin = box[q][0]; ch.ymin = box[q][1]; ch.xmax = box[q][2]; ch.ymax = box[q][3];
+  ch.sx = (ch.xmin + ch.xmax) / 2;
+  ch.sy = (ch.ymin + ch.ymax) / 2;
+  ch.depth = par.depth + 1;
+  return ch;
 }
 
 void Quadtree::split(int node, double const *px, double const *py) {
@@ -119,20 +137,12 @@ void Quadtree::split(int node, double const *px, double const *py) {
     }
     off[q + 1] = i;
   }
-  double const xmin = nodes[node].xmin, ymin = nodes[node].ymin;
-  double const xmax = nodes[node].xmax, ymax = nodes[node].ymax;
-  double const box[4][4] = {{xmin, ymin, sx, sy}, {xmin, sy, sx, ymax},
-                            {sx, ymin, xmax, sy}, {sx, sy, xmax, ymax}};
   int const depth = nodes[node].depth;
   for (int q = 0; q < 4; ++q) {
     int64_t cnt = off[q + 1] - off[q];
     if (cnt == 0) continue;
-    QNode ch;
-    ch.xmin = box[q][0]; ch.ymin = box[q][1]; ch.xmax = box[q][2]; ch.ymax = box[q][3];
-    ch.sx = (ch.xmin + ch.xmax) / 2;
-    ch.sy = (ch.ymin + ch.ymax) / 2;
+    QNode ch = childNode(nodes[node], q);
     ch.parent = node;
-    ch.depth = depth + 1;
     ch.i0 = off[q];
     ch.i1 = off[q + 1];
     int idx = (int)nodes.size();
@@ -490,13 +500,26 @@ void appendOffsets(std::string &out, char const *tag, std::vector<int64_t> const
 }  // namespace
 
 void makePlan(Plan &plan, PlanParams const &params, double const *srcXy,
-              int64_t nSrc, double const *tgtXy, int64_t nTgt) {
+              int64_t nSrc, double const *tgtXy, int64_t nTgt, Quadtree const *srcTree,
+              Quadtree const *tgtTree) {
   if (nSrc < 1 || nTgt < 1) throw std::runtime_error("empty point set");
   if (!(params.k > 0)) throw std::runtime_error("wavenumber must be positive");
   if (!(params.rankEps > 0 && params.rankEps < 1)) throw std::runtime_error("rank eps must be in (0,1)");
   plan = Plan();
-  plan.src.build(srcXy, nSrc, params.leafSize);
-  plan.tgt.build(tgtXy, nTgt, params.leafSize);
+  if (srcTree) {
+    if ((int64_t)srcTree->perm.size() != nSrc || srcTree->leafSize != std::max<int64_t>(1, params.leafSize))
+      throw std::runtime_error("source tree does not match the points");
+    plan.src = *srcTree;
+  } else {
+    plan.src.build(srcXy, nSrc, params.leafSize);
+  }
+  if (tgtTree) {
+    if ((int64_t)tgtTree->perm.size() != nTgt || tgtTree->leafSize != std::max<int64_t>(1, params.leafSize))
+      throw std::runtime_error("target tree does not match the points");
+    plan.tgt = *tgtTree;
+  } else {
+    plan.tgt.build(tgtXy, nTgt, params.leafSize);
+  }
   Planner pl(plan, params);
   plan.root = pl.run();
   // plan order: block-dense children row-major, product factors in stored
@@ -530,7 +553,10 @@ void makePlan(Plan &plan, PlanParams const &params, double const *srcXy,
 
 void makePlanBatched(Plan &plan, PlanParams const &params, double const *k,
                      double const *srcXy, int64_t const *srcOff, double const *tgtXy,
-                     int64_t const *tgtOff, int64_t numProblems) {
+                     int64_t const *tgtOff, int64_t numProblems,
+                     std::vector<Quadtree> const *trees) {
+  if (trees && (int64_t)trees->size() != 2 * numProblems)
+    throw std::runtime_error("one source and one target tree per problem");
   if (numProblems < 1) throw std::runtime_error("no problems");
   std::vector<Plan> subs((size_t)numProblems);
   std::vector<std::string> errs((size_t)numProblems);
@@ -542,7 +568,9 @@ void makePlanBatched(Plan &plan, PlanParams const &params, double const *k,
         PlanParams pp = params;
         pp.k = k[p];
         makePlan(subs[(size_t)p], pp, srcXy + 2 * srcOff[p], srcOff[p + 1] - srcOff[p],
-                 tgtXy + 2 * tgtOff[p], tgtOff[p + 1] - tgtOff[p]);
+                 tgtXy + 2 * tgtOff[p], tgtOff[p + 1] - tgtOff[p],
+                 trees ? &(*trees)[(size_t)(2 * p)] : nullptr,
+                 trees ? &(*trees)[(size_t)(2 * p + 1)] : nullptr);
       } catch (std::exception const &e) {
         errs[(size_t)p] = e.what();
       }

@@ -33,6 +33,11 @@ class Quadtree {
   // leafSize generalises LEAF_SIZE_THRESHOLD = 1 (quadtree_node.c:17): a
   // node with more than leafSize points is split.
   void build(double const *xy, int64_t n, int64_t leafSize);
+  // the root's box from the points' bounding box (bbox.c:18-30) and a
+  // child's box and split point (quadtree_node.c:196-282): the arithmetic
+  // both the host and the GPU build use
+  static QNode rootNode(double xmin, double xmax, double ymin, double ymax);
+  static QNode childNode(QNode const &parent, int q);
   Circle circle(int node) const;  // quadtree_node.c:321-330
   std::vector<int> children(int node) const;
   // LR level order below `node`, grouped by depth (tree_level_iter.c:12-88)
@@ -45,6 +50,13 @@ class Quadtree {
  private:
   void split(int node, double const *px, double const *py);
 };
+
+// Quadtrees of the point sets xy[2 setOff[t] .. 2 setOff[t+1]) built on the
+// GPU (bfg_tree.cu): the same permutation and node table as Quadtree::build
+// of each set.  Synchronises the stream.
+// stream: a cudaStream_t.
+void buildQuadtreesGpu(double const *xy, int64_t const *setOff, int64_t numSets, int64_t leafSize,
+                       void *stream, std::vector<Quadtree> &out);
 
 enum BlockKind : int32_t { kFirst = 0, kMiddle = 1, kLast = 2, kDense = 3 };
 
@@ -118,14 +130,18 @@ struct Plan {
 // srcXy[2*srcOff[p] .. 2*srcOff[p+1]) and targets likewise, wavenumber k[p];
 // the merged plan's rows and columns are the problems' tree orders back to
 // back, and its perms index the concatenated point arrays.
+// trees: null, or the 2 numProblems quadtrees already built (source tree of
+// problem p at 2p, target tree at 2p+1).
 void makePlanBatched(Plan &plan, PlanParams const &params, double const *k,
                      double const *srcXy, int64_t const *srcOff, double const *tgtXy,
-                     int64_t const *tgtOff, int64_t numProblems);
+                     int64_t const *tgtOff, int64_t numProblems,
+                     std::vector<Quadtree> const *trees = nullptr);
 
-// Builds trees and the plan; throws std::runtime_error on geometry the
-// reference cannot factor.
+// Builds trees (unless given) and the plan; throws std::runtime_error on
+// geometry the reference cannot factor.
 void makePlan(Plan &plan, PlanParams const &params, double const *srcXy,
-              int64_t nSrc, double const *tgtXy, int64_t nTgt);
+              int64_t nSrc, double const *tgtXy, int64_t nTgt,
+              Quadtree const *srcTree = nullptr, Quadtree const *tgtTree = nullptr);
 
 // ---------------------------------------------------------------------------
 // GPU descriptor tables

@@ -80,7 +80,8 @@ typedef struct bfgFacOptions {
   int32_t pinvCut;    /* 0: keep sigma >= max(m,n) eps sigma0 + eps
                          (mat_dense_complex.c:1797-1808); 1: keep
                          sigma >= pinvTol * sigma0 (linalg.c:26-36) */
-  int32_t reserved;
+  int32_t treeOnGpu;  /* 1: build the quadtrees on the GPU (the same trees
+                         as the host build, which is the default, 0) */
   double pinvTol;
 } bfgFacOptions;
 
@@ -303,6 +304,31 @@ bfgStatus bfgPlanHelm2(double k, double const *srcXy, int64_t numSrc,
                        bfgFacOptions const *opts, int64_t *srcPerm,
                        int64_t *tgtPerm, char *buf, int64_t capacity,
                        int64_t *length);
+
+/* A quadtree node (BfQuadtreeNode, quadtree_node.h:22-39): bounding box,
+ * split point, the node's points as a range of the tree order, children in
+ * quadrant order (quadtree_node.h:31-37). */
+typedef struct bfgQuadtreeNode {
+  double xmin, ymin, xmax, ymax;
+  double splitX, splitY;
+  int64_t i0, i1;             /* tree-order range of the node's points */
+  int32_t parent, depth;      /* parent -1 at the root */
+  int32_t child[4];           /* -1: no points in that quadrant */
+} bfgQuadtreeNode;
+
+/* bfQuadtreeInit (quadtree.c:80-98) of numSets point sets at once: set t is
+ * xy[2*setOffsets[t] .. 2*setOffsets[t+1]) (host array, setOffsets[0] = 0),
+ * split while a node holds more than leafSize points.  onGpu = 1 builds all
+ * sets on the context's GPU in one breadth-first pass (ctx required), 0 on
+ * the host (ctx may be NULL); both give the same trees, node for node.
+ * perm (setOffsets[numSets] entries) receives each set's tree order as
+ * indices into that set; nodeOffsets (numSets + 1 entries) the range of each
+ * set's nodes in `nodes`, numbered as the reference's recursive build
+ * creates them.  nodes may be NULL to count only; else it has room for
+ * nodeCapacity entries (BFG_ERROR_OUT_OF_RANGE when that is too few). */
+bfgStatus bfgQuadtreeBuild(bfgContext ctx, double const *xy, int64_t const *setOffsets,
+                           int64_t numSets, int64_t leafSize, int32_t onGpu, int64_t *perm,
+                           bfgQuadtreeNode *nodes, int64_t nodeCapacity, int64_t *nodeOffsets);
 
 /* Host-only: the device H0/H1 evaluator's source compiled for the CPU,
  * out[4i..4i+3] = J0, Y0, J1, Y1. */
