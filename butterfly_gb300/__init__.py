@@ -24,7 +24,9 @@ LIB_PATH = os.path.join(_PKG, "libbfg.so")
 
 BFG_OK = 0
 APPLY_ORIGINAL_ORDER = 1
-PRECISIONS = {"fp64": 0, "fp32": 1, "bf16x2": 2, "bf16x3": 3}
+PRECISIONS = {"fp64": 0, "fp32": 1, "bf16x2": 2, "bf16x3": 3, "df64": 4}
+# precisions whose vectors are complex128
+_C128_PRECISIONS = ("fp64", "df64")
 STATUS_NAMES = {0: "OK", 1: "INVALID_ARGUMENTS", 2: "RUNTIME", 3: "NOT_IMPLEMENTED",
                 4: "MEMORY", 5: "OUT_OF_RANGE", 8: "INCOMPATIBLE_SHAPES", 32: "CUDA",
                 33: "TIMEOUT", 34: "NUMERICAL"}
@@ -122,6 +124,7 @@ def lib() -> ctypes.CDLL:
         "bfgPlanHelm2": [ctypes.c_double, _VP, _I64, _VP, _I64, ctypes.POINTER(_FacOptionsC),
                          _VP, _VP, ctypes.c_char_p, _I64, ctypes.POINTER(_I64)],
         "bfgBessel01Host": [_VP, _I64, _VP],
+        "bfgFacPrepare": [_VP, ctypes.c_int32],
         "bfgQuadtreeBuild": [_VP, _VP, _VP, _I64, _I64, ctypes.c_int32, _VP, _VP, _I64, _VP],
         "bfgRngSeed": [ctypes.POINTER(_RngC), ctypes.c_uint64],
         "bfgRngUniform1": [ctypes.POINTER(_RngC)],
@@ -357,6 +360,10 @@ class Fac:
     def __del__(self):
         self.close()
 
+    def prepare(self, precision: str):
+        """Builds the precision's copy of the factors now (bfgFacPrepare)."""
+        self.ctx.check(lib().bfgFacPrepare(self.handle, PRECISIONS[precision]), "prepare")
+
     # -- structure ---------------------------------------------------------
     def perms(self):
         if self._perms is None:
@@ -425,7 +432,7 @@ class Fac:
         import torch
         squeeze = X.dim() == 1
         Xd = X.reshape(X.shape[0], -1)
-        want = torch.complex128 if precision == "fp64" else torch.complex64
+        want = torch.complex128 if precision in _C128_PRECISIONS else torch.complex64
         if Xd.dtype != want or not Xd.is_contiguous():
             Xd = Xd.to(want).contiguous()
         if Xd.shape[0] != self.shape[1]:
@@ -642,6 +649,7 @@ def _solver_sigs():
         "bfgSystemApply": [_VP, _VP, _VP],
         "bfgSystemBuildBlockJacobi": [_VP],
         "bfgSystemApplyBlockJacobi": [_VP, _VP, _VP],
+        "bfgSystemSetApplyPrecision": [_VP, ctypes.c_int32],
         "bfgSolveGmres": [_VP, _VP, _VP, ctypes.c_double, _I64, ctypes.c_int32, _PRECOND_FN,
                           _VP, ctypes.POINTER(_GmresResultC)],
     }
@@ -702,6 +710,16 @@ class System:
             self._check(_solver_sigs().bfgSystemApply(self.handle, _VP(x.data_ptr()),
                                                       _VP(y.data_ptr())), "apply")
         return y
+
+    def set_apply_precision(self, precision: str):
+        """Arithmetic of the butterfly part of the system apply (and so of
+        the GMRES iterations): "fp64" or "df64" (double-float, ~1e-13 of
+        FP64 at FP32 rates).  The solver's final true residual is FP64."""
+        import torch
+        with self.ctx.on_stream(torch.cuda.current_stream().cuda_stream):
+            self._check(_solver_sigs().bfgSystemSetApplyPrecision(self.handle,
+                                                                 PRECISIONS[precision]),
+                        "apply precision")
 
     def build_block_jacobi(self):
         import torch

@@ -76,8 +76,8 @@ struct bfgFac_s {
   // device data
   DevBuf srcPts, tgtPts;            // x, y, nx, ny planes (tree order)
   bool srcHasNormals = false, tgtHasNormals = false;
-  DevBuf arena64, arena32;
-  bool arena32Ready = false;
+  DevBuf arena64, arena32, arenaDf;
+  bool arena32Ready = false, arenaDfReady = false;
   DevBuf srcPerm, tgtPerm;
   DevBuf items, contribs, rowSeg, segStart, segContrib0, segBase;
   DevBuf ws, xbuf;
@@ -447,6 +447,52 @@ void ensureArena32(bfgFac f) {
   f->arena32Ready = true;
 }
 
+void ensureArenaDf(bfgFac f) {
+  if (f->arenaDfReady) return;
+  int64_t n = std::max<int64_t>(1, f->plan.arenaEntries);
+  ck(f->arenaDf.ensure((size_t)n * sizeof(float4)), "double-float arena");
+  ck(bfg::launchArenaToDf(f->arena64.as<double2>(), f->arenaDf.as<float4>(), f->plan.arenaEntries,
+                          f->ctx->stream),
+     "double-float arena");
+  f->arenaDfReady = true;
+}
+
+// the double-float apply: input split (and gathered) into the X buffer,
+// stages on double-float rows, final sum into complex128 Y.  Same launch
+// count as runApply (the split stands in for its gather; without
+// BFG_APPLY_ORIGINAL_ORDER it is timed with the first stage).
+void runApplyDf(bfgFac f, double2 const *X, int64_t ldx, int64_t R, double2 *Y, int64_t ldy,
+                uint32_t flags, std::vector<cudaEvent_t> *events) {
+  cudaStream_t s = f->ctx->stream;
+  bfg::ApplyProgram const &p = f->prog;
+  ck(f->ws.ensure((size_t)std::max<int64_t>(1, p.wsRows) * R * sizeof(float4)), "workspace");
+  ck(f->xbuf.ensure((size_t)std::max<int64_t>(1, p.numCols) * R * sizeof(float4)), "input buffer");
+  float4 *W = f->ws.as<float4>(), *Xd = f->xbuf.as<float4>();
+  size_t ev = 0;
+  auto mark = [&]() {
+    if (events) ck(cudaEventRecord((*events)[ev++], s), "event");
+  };
+  bool const orig = (flags & BFG_APPLY_ORIGINAL_ORDER) != 0;
+  mark();
+  ck(bfg::launchGatherToDf(X, ldx, orig ? f->srcPerm.as<int64_t>() : nullptr, p.numCols, R, Xd, s),
+     "split X");
+  if (orig) mark();
+  size_t const nStages = f->stageItem0.size() - 1;
+  for (size_t st = 0; st < nStages; ++st) {
+    int64_t a = f->stageItem0[st], b = f->stageItem0[st + 1];
+    ck(bfg::launchApplyStageDf(f->items.as<bfg::ApplyItem>() + a, b - a,
+                               f->contribs.as<bfg::ApplyContrib>(), f->arenaDf.as<float4>(), Xd,
+                               W, R, s),
+       "apply stage");
+    mark();
+  }
+  ck(bfg::launchApplyReduceDf(f->rowSeg.as<int32_t>(), f->segStart.as<int64_t>(),
+                              f->segContrib0.as<int64_t>(), f->segBase.as<int64_t>(), W, R, Y,
+                              ldy, p.numRows, orig ? f->tgtPerm.as<int64_t>() : nullptr, s),
+     "apply reduce");
+  mark();
+}
+
 void keepInputs(bfgFac f, double const *srcXy, double const *srcN, int64_t nSrc,
                 double const *tgtXy, double const *tgtN, int64_t nTgt, double const *k,
                 int64_t numProblems, int64_t const *srcOff, int64_t const *tgtOff) {
@@ -557,6 +603,7 @@ void runApplyTc(bfgFac f, int terms, float2 const *X, int64_t ldx, int64_t R, fl
 // one-time preparation of a precision's copy of the factors
 void preparePrecision(bfgFac f, bfgPrecision prec) {
   if (prec == BFG_PRECISION_FP32) ensureArena32(f);
+  if (prec == BFG_PRECISION_DF64) ensureArenaDf(f);
   if (prec == BFG_PRECISION_BF16X2) ensureTc(f, 2);
   if (prec == BFG_PRECISION_BF16X3) ensureTc(f, 3);
 }
@@ -574,6 +621,10 @@ bfgStatus applyDispatch(bfgFac f, bfgPrecision prec, void const *X, int64_t ldx,
     ensureArena32(f);
     runApply<float2>(f, f->arena32.as<float2>(), static_cast<float2 const *>(X), ldx, R,
                      static_cast<float2 *>(Y), ldy, flags, ev);
+  } else if (prec == BFG_PRECISION_DF64) {
+    ensureArenaDf(f);
+    runApplyDf(f, static_cast<double2 const *>(X), ldx, R, static_cast<double2 *>(Y), ldy, flags,
+               ev);
   } else if (isTcPrecision(prec)) {
     int const terms = prec == BFG_PRECISION_BF16X3 ? 3 : 2;
     ensureTc(f, terms);
@@ -1179,7 +1230,7 @@ bfgStatus bfgFacApplyHost(bfgFac f, bfgPrecision prec, double const *X, int64_t 
     ck(cudaMemcpy2DAsync(f->hx128.p, (size_t)R * 16, X, (size_t)ldx * 16, (size_t)R * 16,
                          (size_t)nc, cudaMemcpyHostToDevice, s),
        "copy X");
-    if (prec == BFG_PRECISION_FP64) {
+    if (prec == BFG_PRECISION_FP64 || prec == BFG_PRECISION_DF64) {
       bfgStatus st = applyDispatch(f, prec, f->hx128.p, R, R, f->hy128.p, R, flags, nullptr);
       if (st != BFG_OK) return st;
     } else if (prec == BFG_PRECISION_FP32 || isTcPrecision(prec)) {
@@ -1199,6 +1250,17 @@ bfgStatus bfgFacApplyHost(bfgFac f, bfgPrecision prec, double const *X, int64_t 
        "copy Y");
     ck(cudaStreamSynchronize(s), "apply");
     if (isTcPrecision(prec)) checkTcStatus(f);
+    return BFG_OK;
+  });
+}
+
+bfgStatus bfgFacPrepare(bfgFac f, bfgPrecision prec) {
+  if (!f) return BFG_ERROR_INVALID_ARGUMENTS;
+  if (prec < BFG_PRECISION_FP64 || prec > BFG_PRECISION_DF64)
+    return fail(f->ctx, BFG_ERROR_INVALID_ARGUMENTS, "prepare: unknown precision");
+  return guarded(f->ctx, [&]() -> bfgStatus {
+    preparePrecision(f, prec);
+    ck(cudaStreamSynchronize(f->ctx->stream), "prepare");
     return BFG_OK;
   });
 }

@@ -76,6 +76,18 @@ cudaError_t launchBessel01(double const *x, int64_t n, double *out, cudaStream_t
 
 // FP64 -> FP32 arena conversion (same layout)
 cudaError_t launchArenaToF32(double2 const *a64, float2 *a32, int64_t n, cudaStream_t stream);
+// double-float apply (bfg_df64.cu): arena split, input split (and gather),
+// stage, final sum into complex128
+cudaError_t launchArenaToDf(double2 const *a64, float4 *adf, int64_t n, cudaStream_t stream);
+cudaError_t launchGatherToDf(double2 const *X, int64_t ldx, int64_t const *perm, int64_t nRows,
+                             int64_t R, float4 *out, cudaStream_t stream);
+cudaError_t launchApplyStageDf(ApplyItem const *items, int64_t nItems,
+                               ApplyContrib const *contribs, float4 const *arena,
+                               float4 const *X, float4 *W, int64_t R, cudaStream_t stream);
+cudaError_t launchApplyReduceDf(int32_t const *rowSeg, int64_t const *segStart,
+                                int64_t const *segContrib0, int64_t const *segBase,
+                                float4 const *W, int64_t R, double2 *Y, int64_t ldy,
+                                int64_t nRows, int64_t const *outPerm, cudaStream_t stream);
 
 // complex128 <-> complex64 matrix conversion (row-major, leading dims)
 cudaError_t launchC128ToC64(double2 const *a, int64_t lda, int64_t rows, int64_t cols,

@@ -281,46 +281,146 @@ __global__ void blockDiagApplyKernel(int64_t n, int64_t const *curveOf, int64_t 
   if (lane == 0) z[row] = make_double2(sr, si);
 }
 
-// h[i] = sum_r conj(V_i[r]) w[r], i < k (V_i at V + i*ldv); one CTA per i
-__global__ void multiDotKernel(int64_t n, double2 const *V, int64_t ldv, int k, double2 const *w,
-                               double2 *h) {
-  int const i = blockIdx.x;
-  if (i >= k) return;
+// The same product from an FP32 copy of the inverses, FP32 arithmetic: the
+// preconditioner inside flexible GMRES (its accuracy does not change the
+// solution the solver converges to, only possibly the iteration count).
+__global__ void blockDiagApply32Kernel(int64_t n, int64_t const *curveOf, int64_t const *offsets,
+                                       int64_t const *blkOff, float2 const *inv, double2 const *r,
+                                       double2 *z) {
+  int64_t const row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= n) return;
+  int const lane = threadIdx.x & 31;
+  int64_t const b = curveOf[row];
+  int64_t const i0 = offsets[b], m = offsets[b + 1] - i0;
+  float2 const *a = inv + blkOff[b] + (row - i0) * m;
+  float sr = 0.f, si = 0.f;
+  for (int64_t j = lane; j < m; j += 32) {
+    float2 const c = a[j];
+    double2 const rv = r[i0 + j];
+    float const vx = (float)rv.x, vy = (float)rv.y;
+    sr += c.x * vx - c.y * vy;
+    si += c.x * vy + c.y * vx;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sr += __shfl_xor_sync(0xffffffffu, sr, o);
+    si += __shfl_xor_sync(0xffffffffu, si, o);
+  }
+  if (lane == 0) z[row] = make_double2(sr, si);
+}
+
+__global__ void c128ToC64FlatKernel(int64_t n, double2 const *a, float2 *b) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+
+// h[i] = sum_r conj(V_i[r]) w[r], i < k, in two steps: CTA (c, i) sums the
+// products of vector i over row chunk c (1,024 rows, 4 per thread) into one
+// partial; then each vector's partials are added over the chunks in order.
+// One CTA per (chunk, vector) keeps every SM busy: the FP64 work of
+// classical Gram-Schmidt needs all of GB300's FP64 units.
+constexpr int kDotThreads = 256, kDotRows = 4 * kDotThreads;
+__global__ void __launch_bounds__(kDotThreads)
+multiDotPartKernel(int64_t n, double2 const *V, int64_t ldv, int k, double2 const *w,
+                   double2 *part, int32_t const *gate) {
+  if (gate && !*gate) return;   // a skipped reorthogonalisation pass
+  __shared__ double red[2][kDotThreads / 32];
+  int64_t const r0 = blockIdx.x * (int64_t)kDotRows;
+  int const i = blockIdx.y;
   double2 const *v = V + (int64_t)i * ldv;
   double sr = 0, si = 0;
-  for (int64_t r = threadIdx.x; r < n; r += blockDim.x) {
-    double2 a = v[r], b = w[r];
-    sr += a.x * b.x + a.y * b.y;
-    si += a.x * b.y - a.y * b.x;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    int64_t const r = r0 + q * kDotThreads + threadIdx.x;
+    if (r < n) {
+      double2 const a = v[r], b = w[r];
+      sr += a.x * b.x + a.y * b.y;
+      si += a.x * b.y - a.y * b.x;
+    }
   }
-  __shared__ double rr[32], ri[32];
   for (int o = 16; o > 0; o >>= 1) {
     sr += __shfl_xor_sync(0xffffffffu, sr, o);
     si += __shfl_xor_sync(0xffffffffu, si, o);
   }
   int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0) { rr[warp] = sr; ri[warp] = si; }
+  if (lane == 0) {
+    red[0][warp] = sr;
+    red[1][warp] = si;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     double a = 0, c = 0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { a += rr[q]; c += ri[q]; }
-    h[i] = make_double2(a, c);
+    for (int q = 0; q < kDotThreads / 32; ++q) {
+      a += red[0][q];
+      c += red[1][q];
+    }
+    part[blockIdx.x * (int64_t)k + i] = make_double2(a, c);
   }
 }
+__global__ void multiDotFinishKernel(int nChunks, int k, double2 const *part, double2 *h,
+                                     int32_t const *gate) {
+  int const i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= k) return;
+  if (gate && !*gate) {
+    h[i] = make_double2(0, 0);
+    return;
+  }
+  double sr = 0, si = 0;
+  for (int c = 0; c < nChunks; ++c) {
+    double2 const v = part[(int64_t)c * k + i];
+    sr += v.x;
+    si += v.y;
+  }
+  h[i] = make_double2(sr, si);
+}
+int dotChunks(int64_t n) { return (int)((n + kDotRows - 1) / kDotRows); }
 
-// w += sign * sum_{i<k} V_i h_i
-__global__ void multiAxpyKernel(int64_t n, double2 const *V, int64_t ldv, int k,
-                                double2 const *h, double sign, double2 *w) {
-  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n;
-       r += (int64_t)gridDim.x * blockDim.x) {
-    double sr = 0, si = 0;
-    for (int i = 0; i < k; ++i) {
+// w += sign * sum_{i<k} V_i h_i.  A CTA takes 32 rows; its 16 warps split
+// the k basis vectors (warp s takes i = s, s + 16, ...), each warp reading
+// 32 consecutive rows of a vector, and the 16 partial sums are added in a
+// fixed order.
+constexpr int kAxpyRows = 32, kAxpySlices = 16;
+__global__ void __launch_bounds__(kAxpyRows * kAxpySlices)
+multiAxpyKernel(int64_t n, double2 const *V, int64_t ldv, int k, double2 const *h, double sign,
+                double2 *w, int32_t const *gate) {
+  if (gate && !*gate) return;
+  __shared__ double2 part[kAxpySlices][kAxpyRows];
+  int const lr = threadIdx.x % kAxpyRows, sl = threadIdx.x / kAxpyRows;
+  int64_t const r = blockIdx.x * (int64_t)kAxpyRows + lr;
+  double sr = 0, si = 0;
+  if (r < n)
+    for (int i = sl; i < k; i += kAxpySlices) {
       double2 const a = V[(int64_t)i * ldv + r], c = h[i];
       sr += a.x * c.x - a.y * c.y;
       si += a.x * c.y + a.y * c.x;
     }
-    w[r] = make_double2(w[r].x + sign * sr, w[r].y + sign * si);
+  part[sl][lr] = make_double2(sr, si);
+  __syncthreads();
+  if (sl == 0 && r < n) {
+    double tr = 0, ti = 0;
+#pragma unroll
+    for (int q = 0; q < kAxpySlices; ++q) {
+      tr += part[q][lr].x;
+      ti += part[q][lr].y;
+    }
+    w[r] = make_double2(w[r].x + sign * tr, w[r].y + sign * ti);
   }
+}
+int axpyGrid(int64_t n) { return (int)((n + kAxpyRows - 1) / kAxpyRows); }
+
+// DGKS criterion: a second Gram-Schmidt pass when the first removed more
+// than half of w's squared norm (||w_after|| < ||w_before|| / sqrt 2)
+__global__ void reorthGateKernel(double2 const *before, double2 const *after, int32_t *gate) {
+  *gate = after->x < 0.5 * before->x ? 1 : 0;
+}
+
+// y = x / sqrt(nrm2->x) (0 if the norm is 0), the norm read on the device
+__global__ void scaleByNormKernel(int64_t n, double2 const *nrm2, double2 const *x, double2 *y) {
+  double const q = nrm2->x;
+  double const s = q > 0 ? 1.0 / sqrt(q) : 0.0;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n;
+       r += (int64_t)gridDim.x * blockDim.x)
+    y[r] = make_double2(s * x[r].x, s * x[r].y);
 }
 
 __global__ void scaleCopyKernel(int64_t n, double s, double2 const *x, double2 *y) {
@@ -365,6 +465,7 @@ struct bfgSystem_s {
   int64_t n = 0, numCurves = 0;
   int32_t order = 0;
   double shift = 0.5;
+  bfgPrecision applyPrec = BFG_PRECISION_FP64;   // of the butterfly part
   bfg::KernelParams kp{};
   std::vector<int64_t> offsets;
   Dev dOffsets, dCurveOf, dX, dW, dKrVal, dKrCol;
@@ -372,7 +473,7 @@ struct bfgSystem_s {
   // block-Jacobi
   bool haveBj = false;
   std::vector<int64_t> blkOff;
-  Dev dBlkOff, dInv, dWork, dColBuf, dFlag;
+  Dev dBlkOff, dInv, dInv32, dWork, dColBuf, dFlag;
   std::string err;
   cudaStream_t stream() const;
 };
@@ -486,15 +587,34 @@ bfgStatus bfgSystemDestroy(bfgSystem sys) {
 
 char const *bfgSystemGetErrorString(bfgSystem sys) { return sys ? sys->err.c_str() : "no system"; }
 
+namespace {
+bfgStatus systemApply(bfgSystem sys, bfgPrecision prec, void const *X, void *Y);
+}
+
 bfgStatus bfgSystemApply(bfgSystem sys, void const *X, void *Y) {
   if (!sys || !X || !Y) return BFG_ERROR_INVALID_ARGUMENTS;
+  return systemApply(sys, sys->applyPrec, X, Y);
+}
+
+bfgStatus bfgSystemSetApplyPrecision(bfgSystem sys, bfgPrecision prec) {
+  if (!sys) return BFG_ERROR_INVALID_ARGUMENTS;
+  if (prec != BFG_PRECISION_FP64 && prec != BFG_PRECISION_DF64)
+    return sysFail(sys, BFG_ERROR_INVALID_ARGUMENTS, "system: FP64 or DF64 applies only");
+  bfgStatus st = bfgFacPrepare(sys->fac, prec);
+  if (st != BFG_OK) return sysFail(sys, st, "system: preparing the factors failed");
+  sys->applyPrec = prec;
+  return BFG_OK;
+}
+
+namespace {
+bfgStatus systemApply(bfgSystem sys, bfgPrecision prec, void const *X, void *Y) {
   cudaStream_t s = sys->stream();
   int64_t const n = sys->n;
   double2 const *x = static_cast<double2 const *>(X);
   double2 *xw = sys->tmpXw.as<double2>(), *kxw = sys->tmpK.as<double2>();
   scaleKernel<<<gridFor(n, 256), 256, 0, s>>>(n, sys->dW.as<double>(), x, xw);
   SYS_CK(cudaGetLastError());
-  bfgStatus st = bfgFacApply(sys->fac, BFG_PRECISION_FP64, xw, 1, 1, kxw, 1, BFG_APPLY_ORIGINAL_ORDER);
+  bfgStatus st = bfgFacApply(sys->fac, prec, xw, 1, 1, kxw, 1, BFG_APPLY_ORIGINAL_ORDER);
   if (st != BFG_OK) return sysFail(sys, st, "system apply: butterfly apply failed");
   systemPostKernel<<<gridFor(n, 256), 256, 0, s>>>(n, sys->shift, x, xw, kxw,
                                                    sys->dKrVal.as<double2>(),
@@ -503,6 +623,7 @@ bfgStatus bfgSystemApply(bfgSystem sys, void const *X, void *Y) {
   SYS_CK(cudaGetLastError());
   return BFG_OK;
 }
+}  // namespace
 
 bfgStatus bfgSystemBuildBlockJacobi(bfgSystem sys) {
   if (!sys) return BFG_ERROR_INVALID_ARGUMENTS;
@@ -544,6 +665,10 @@ bfgStatus bfgSystemBuildBlockJacobi(bfgSystem sys) {
   SYS_CK(cudaMemcpyAsync(&flag, sys->dFlag.p, 4, cudaMemcpyDeviceToHost, s));
   SYS_CK(cudaStreamSynchronize(s));
   if (flag) return sysFail(sys, BFG_ERROR_NUMERICAL, "block-Jacobi: a diagonal block is singular");
+  SYS_CK(sys->dInv32.alloc(tot * 8));
+  c128ToC64FlatKernel<<<gridFor(tot, 256), 256, 0, s>>>(tot, sys->dInv.as<double2>(),
+                                                        sys->dInv32.as<float2>());
+  SYS_CK(cudaGetLastError());
   sys->haveBj = true;
   return BFG_OK;
 }
@@ -578,14 +703,28 @@ bfgStatus bfgSolveGmres(bfgSystem sys, void const *B, void *X, double tol, int64
   SYS_CK(Z.alloc((size_t)m * n * 16));
   SYS_CK(w.alloc(n * 16));
   SYS_CK(r.alloc(n * 16));
-  SYS_CK(h.alloc((m + 2) * 16));
+  SYS_CK(h.alloc((2 * m + 4) * 16));
+  Dev dotPart;
+  int const nChunks = dotChunks(n);
+  SYS_CK(dotPart.alloc((size_t)nChunks * (m + 1) * 16));
+  // h_out[i] = (V_i, w) for i < k
+  Dev gateBuf;
+  SYS_CK(gateBuf.alloc(4));
+  int32_t *gate = gateBuf.as<int32_t>();
+  auto dots = [&](double2 const *Vm, int k, double2 const *wv, double2 *hOut,
+                  int32_t const *g = nullptr) {
+    multiDotPartKernel<<<dim3((unsigned)nChunks, (unsigned)k), kDotThreads, 0, s>>>(
+        n, Vm, n, k, wv, dotPart.as<double2>(), g);
+    multiDotFinishKernel<<<(k + 127) / 128, 128, 0, s>>>(nChunks, k, dotPart.as<double2>(), hOut,
+                                                         g);
+  };
   double2 *Vp = V.as<double2>(), *Zp = Z.as<double2>(), *wp = w.as<double2>(), *rp = r.as<double2>();
   double2 *hp = h.as<double2>();
   double2 *xp = static_cast<double2 *>(X);
   double2 const *bp = static_cast<double2 const *>(B);
 
   auto norm = [&](double2 const *v, double *out) -> bfgStatus {
-    multiDotKernel<<<1, 512, 0, s>>>(n, v, n, 1, v, hp);
+    dots(v, 1, v, hp);
     SYS_CK(cudaGetLastError());
     double2 hv;
     SYS_CK(cudaMemcpyAsync(&hv, hp, 16, cudaMemcpyDeviceToHost, s));
@@ -598,7 +737,13 @@ bfgStatus bfgSolveGmres(bfgSystem sys, void const *B, void *X, double tol, int64
       SYS_CK(cudaMemcpyAsync(outv, in, n * 16, cudaMemcpyDeviceToDevice, s));
       return BFG_OK;
     }
-    if (precond == BFG_PRECOND_BLOCK_JACOBI) return bfgSystemApplyBlockJacobi(sys, in, outv);
+    if (precond == BFG_PRECOND_BLOCK_JACOBI) {
+      blockDiagApply32Kernel<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(
+          n, sys->dCurveOf.as<int64_t>(), sys->dOffsets.as<int64_t>(),
+          sys->dBlkOff.as<int64_t>(), sys->dInv32.as<float2>(), in, outv);
+      SYS_CK(cudaGetLastError());
+      return BFG_OK;
+    }
     bfgStatus st = userFn(userData, in, outv, (void *)s);
     return st == BFG_OK ? st : sysFail(sys, st, "user preconditioner failed");
   };
@@ -620,7 +765,7 @@ bfgStatus bfgSolveGmres(bfgSystem sys, void const *B, void *X, double tol, int64
 
   std::vector<cd> H((size_t)(m + 1) * m, cd(0)), g(m + 1, cd(0)), cs(m), sn(m);
   g[0] = beta;
-  std::vector<double2> hh(m + 2);
+  std::vector<double2> hh(2 * m + 4);
   int64_t j = 0;
   double res = beta / bnorm;
   bool converged = res < tol;
@@ -628,21 +773,30 @@ bfgStatus bfgSolveGmres(bfgSystem sys, void const *B, void *X, double tol, int64
     double2 *vj = Vp + j * n, *zj = Zp + j * n;
     if ((st = applyM(vj, zj)) != BFG_OK) return st;
     if ((st = bfgSystemApply(sys, zj, wp)) != BFG_OK) return st;
-    // classical Gram-Schmidt, twice
+    // classical Gram-Schmidt with a second pass where the DGKS criterion
+    // asks for it, the norm and the next basis vector, all on the device;
+    // one read of the Hessenberg column per iteration (h: passes 1 and 2 in
+    // slots [0, k) and [k, 2k), ||w||^2 in slot 2k, before / after pass 1
+    // in slots 2k+1, 2k+2)
     int const k = (int)(j + 1);
     std::vector<cd> hcol(k + 1, cd(0));
-    for (int pass = 0; pass < 2; ++pass) {
-      multiDotKernel<<<k, 512, 0, s>>>(n, Vp, n, k, wp, hp);
-      multiAxpyKernel<<<gridFor(n, 256), 256, 0, s>>>(n, Vp, n, k, hp, -1.0, wp);
-      SYS_CK(cudaGetLastError());
-      SYS_CK(cudaMemcpyAsync(hh.data(), hp, k * 16, cudaMemcpyDeviceToHost, s));
-      SYS_CK(cudaStreamSynchronize(s));
-      for (int i = 0; i < k; ++i) hcol[i] += cd(hh[i].x, hh[i].y);
-    }
-    double wn = 0;
-    if ((st = norm(wp, &wn)) != BFG_OK) return st;
+    dots(wp, 1, wp, hp + 2 * k + 1);
+    dots(Vp, k, wp, hp);
+    multiAxpyKernel<<<axpyGrid(n), kAxpyRows * kAxpySlices, 0, s>>>(n, Vp, n, k, hp, -1.0, wp,
+                                                                    nullptr);
+    dots(wp, 1, wp, hp + 2 * k + 2);
+    reorthGateKernel<<<1, 1, 0, s>>>(hp + 2 * k + 1, hp + 2 * k + 2, gate);
+    dots(Vp, k, wp, hp + k, gate);
+    multiAxpyKernel<<<axpyGrid(n), kAxpyRows * kAxpySlices, 0, s>>>(n, Vp, n, k, hp + k, -1.0,
+                                                                    wp, gate);
+    dots(wp, 1, wp, hp + 2 * k);
+    scaleByNormKernel<<<gridFor(n, 256), 256, 0, s>>>(n, hp + 2 * k, wp, Vp + (j + 1) * n);
+    SYS_CK(cudaGetLastError());
+    SYS_CK(cudaMemcpyAsync(hh.data(), hp, (2 * k + 1) * 16, cudaMemcpyDeviceToHost, s));
+    SYS_CK(cudaStreamSynchronize(s));
+    for (int i = 0; i < k; ++i) hcol[i] = cd(hh[i].x + hh[k + i].x, hh[i].y + hh[k + i].y);
+    double const wn = std::sqrt(std::max(0.0, hh[2 * k].x));
     hcol[k] = wn;
-    if (wn > 0) scaleCopyKernel<<<gridFor(n, 256), 256, 0, s>>>(n, 1.0 / wn, wp, Vp + (j + 1) * n);
     // apply previous rotations, then a new one (linalg.c:202-227)
     for (int64_t i = 0; i < j; ++i) {
       cd const a = hcol[i], b = hcol[i + 1];
@@ -677,11 +831,12 @@ bfgStatus bfgSolveGmres(bfgSystem sys, void const *B, void *X, double tol, int64
     std::vector<double2> yd(j);
     for (int64_t i = 0; i < j; ++i) yd[i] = make_double2(yv[i].real(), yv[i].imag());
     SYS_CK(cudaMemcpyAsync(hp, yd.data(), j * 16, cudaMemcpyHostToDevice, s));
-    multiAxpyKernel<<<gridFor(n, 256), 256, 0, s>>>(n, Zp, n, (int)j, hp, 1.0, xp);
+    multiAxpyKernel<<<axpyGrid(n), kAxpyRows * kAxpySlices, 0, s>>>(n, Zp, n, (int)j, hp, 1.0, xp,
+                                                                    nullptr);
     SYS_CK(cudaGetLastError());
   }
-  // true residual
-  if ((st = bfgSystemApply(sys, xp, rp)) != BFG_OK) return st;
+  // true residual, with the FP64 apply whatever the iterations used
+  if ((st = systemApply(sys, BFG_PRECISION_FP64, xp, rp)) != BFG_OK) return st;
   subFromKernel<<<gridFor(n, 256), 256, 0, s>>>(n, bp, rp);
   double rn = 0;
   if ((st = norm(rp, &rn)) != BFG_OK) return st;

@@ -54,7 +54,12 @@ typedef enum bfgPrecision {
    * BF16X3 stores 12 bytes and keeps ~24 bits (FP32-like).  The reference
    * computes in complex128 only; these are GB300 additions. */
   BFG_PRECISION_BF16X2 = 2,
-  BFG_PRECISION_BF16X3 = 3
+  BFG_PRECISION_BF16X3 = 3,
+  /* complex128 vectors in and out, factors and intermediates as pairs of
+   * FP32 numbers (hi + lo, ~48 significant bits, 16 bytes per complex
+   * entry) with error-free FP32 products: within ~1e-13 of FP64 at FP32
+   * rates.  A GB300 addition (its FP64 units run at 1/64 of FP32). */
+  BFG_PRECISION_DF64 = 4
 } bfgPrecision;
 
 typedef struct bfgContext_s *bfgContext;
@@ -175,6 +180,10 @@ bfgStatus bfgFacCopyBlocks(bfgFac fac, double *entries, int64_t capacityEntries,
 /* Flags of the applies. */
 #define BFG_APPLY_ORIGINAL_ORDER 1u  /* X and Y rows in original point order */
 
+/* Builds the precision's copy of the factors now, as the first apply in that
+ * precision would (allocates and synchronises). */
+bfgStatus bfgFacPrepare(bfgFac fac, bfgPrecision precision);
+
 /* Y = A X -- bfMatMul (mat.c:183-185) with A the factorization.  X (numCols
  * x numRhs) and Y (numRows x numRhs) are DEVICE pointers: complex128 for
  * FP64, complex64 for FP32, BF16X2 and BF16X3.  The first apply in a
@@ -265,6 +274,10 @@ char const *bfgSystemGetErrorString(bfgSystem sys);
 /* Y = A X for one device complex128 vector (bfMatMul on the assembled
  * operator). */
 bfgStatus bfgSystemApply(bfgSystem sys, void const *X, void *Y);
+/* Arithmetic of the butterfly part of bfgSystemApply, and so of the GMRES
+ * iterations: BFG_PRECISION_FP64 (the default) or BFG_PRECISION_DF64.
+ * bfgSolveGmres computes its final true residual in FP64 either way. */
+bfgStatus bfgSystemSetApplyPrecision(bfgSystem sys, bfgPrecision precision);
 /* Block-Jacobi preconditioner: dense diagonal block of A per curve, inverted
  * on the GPU (assemblePreconditioner, multiple_scattering_context.c:545-634;
  * the reference factors them with zgetrf, lu_dense_complex.c:185-232). */
@@ -289,7 +302,10 @@ typedef struct bfgGmresResult {
 
 /* Solves A x = b with right-preconditioned flexible GMRES (no restart, at
  * most maxIter iterations), X holding x0 on entry and x on exit (device
- * complex128).  Replaces bfSolveGMRES (linalg.c:47-317), which is
+ * complex128).  Arnoldi in FP64: classical Gram-Schmidt with a second pass
+ * where the DGKS criterion asks for one; BFG_PRECOND_BLOCK_JACOBI applies
+ * an FP32 copy of the block inverses (a flexible solver's preconditioner
+ * needs no more).  Replaces bfSolveGMRES (linalg.c:47-317), which is
  * left-preconditioned: here the convergence test |g_{j+1}|/||b|| < tol is
  * on the true residual. */
 bfgStatus bfgSolveGmres(bfgSystem sys, void const *B, void *X, double tol,

@@ -83,7 +83,10 @@ def test_preconditioning_reduces_iterations_and_user_callback(problem):
     _, i_bj = B.solve_gmres(sys_, bt, tol=1e-8, max_num_iter=400, precond="block_jacobi")
     _, i_cb = B.solve_gmres(sys_, bt, tol=1e-8, max_num_iter=400, precond=user)
     assert i_bj["iterations"] < i_none["iterations"]
-    assert i_cb["iterations"] == i_bj["iterations"]
+    # the built-in preconditioner applies an FP32 copy of the same inverses
+    # (the callback here uses the FP64 ones): a flexible solver may take an
+    # iteration more or less, no more
+    assert abs(i_cb["iterations"] - i_bj["iterations"]) <= 2
     assert i_cb["trueRelResidual"] < 1e-7
 
 
@@ -100,3 +103,25 @@ def test_kr_correction_restates_reference(problem):
     j = (i + 1) % m
     k = O.kernel_pairs(h, pts[[i]], nrm[[i]], pts[[j]])[0]
     assert np.isclose(v[sel][0], O.KR_WEIGHTS[6][0] * k)
+
+
+def test_df64_system_apply_and_gmres(problem):
+    """Double-float matvecs (FP32 arithmetic, ~48 bits): the system apply
+    within 1e-12 of FP64, and FGMRES on them reaches the same solution with a
+    true FP64 residual below the tolerance."""
+    A, sys_, b = problem["A"], problem["sys"], problem["b"]
+    x = torch.from_numpy(O.RefRng(12).complex_randn(A.shape[0])).cuda()
+    y64 = sys_.apply(x)
+    sys_.set_apply_precision("df64")
+    try:
+        ydf = sys_.apply(x)
+        assert rel_err(ydf.cpu().numpy(), y64.cpu().numpy()) < 1e-12
+        sys_.build_block_jacobi()
+        xs, info = B.solve_gmres(sys_, torch.from_numpy(b).cuda(), tol=1e-10, max_num_iter=400,
+                                 precond="block_jacobi")
+    finally:
+        sys_.set_apply_precision("fp64")
+    assert info["converged"] == 1 and info["trueRelResidual"] < 1e-9
+    assert rel_err(xs.cpu().numpy(), np.linalg.solve(A, b)) < 1e-7
+    with pytest.raises(B.BfgError):
+        sys_.set_apply_precision("fp32")

@@ -102,3 +102,36 @@ def test_tensor_apply_timed_launch_count(ctx):
     ms = fac.apply_timed(X.data_ptr(), 16, 16, Y.data_ptr(), 16, "bf16x3")
     assert len(ms) == len(fac.launch_info())
     assert torch.count_nonzero(Y).item() == 0
+
+
+# ---- double-float (df64): FP64 accuracy from FP32 arithmetic ----
+@pytest.mark.parametrize("R", [1, 3, 16])
+def test_df64_apply_matches_fp64(ctx, R):
+    g, fac = golden_fac("ellipse_n16384_k128", ctx)
+    n = fac.shape[1]
+    X = torch.from_numpy(O.RefRng(31 + R).complex_randn(n * R).reshape(n, R)).cuda()
+    y64 = fac.apply(X)
+    ydf = fac.apply(X, precision="df64")
+    assert ydf.dtype == torch.complex128
+    # double-float keeps ~48 significant bits: agreement far below FP32's
+    assert rel_err(ydf.cpu().numpy(), y64.cpu().numpy()) < 1e-12
+
+
+def test_df64_apply_reference_output_and_original_order(ctx):
+    g, fac = golden_fac("star_n2048_k48", ctx)
+    y = fac.apply(g["x"], precision="df64")                # host complex128 path
+    assert rel_err(y, g["y_bf"].reshape(y.shape)) < 1e-12
+    sp, tp = fac.perms()
+    x_orig = np.empty_like(g["x"])
+    x_orig[sp] = g["x"]
+    y_orig = fac.apply(x_orig, precision="df64", original_order=True)
+    assert np.array_equal(y_orig[tp], y)
+
+
+def test_df64_apply_is_deterministic_and_timed(ctx):
+    g, fac = golden_fac("star_n2048_k48", ctx)
+    X = torch.from_numpy(O.RefRng(8).complex_randn(2048 * 2).reshape(2048, 2)).cuda()
+    assert torch.equal(fac.apply(X, precision="df64"), fac.apply(X, precision="df64"))
+    Y = torch.empty_like(X)
+    ms = fac.apply_timed(X.data_ptr(), 2, 2, Y.data_ptr(), 2, "df64")
+    assert len(ms) == len(fac.launch_info())
