@@ -75,6 +75,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-gmres", action="store_true",
                     help="skip the multiple-scattering GMRES time-to-1e-8 measurement")
+    ap.add_argument("--learned", action="store_true",
+                    help="also train the learned preconditioner on GMRES solves of other "
+                         "scatterer layouts and compare it with block-Jacobi (about a minute)")
     return ap.parse_args()
 
 
@@ -401,6 +404,71 @@ def gmres_scattering(B, ctx):
             "factorization_s": fac_s, "block_jacobi_setup_s": bj_s}
 
 
+def learned_scattering(B, ctx, train_layouts=6, angles=6, iterates=(0, 20, 60, 150),
+                       epochs=30, chunk=64):
+    """The learned preconditioner on the C5 problem: a 4 chunk -> 256 -> 256
+    -> 2 chunk network trained (hand-written kernels, Adam) on pairs from
+    block-Jacobi GMRES solves on other scatterer layouts (seeds 1..6, random
+    angles), then FGMRES to 1e-8 on the bench layout (seed 0) and a held-out
+    one (seed 7) with block-Jacobi alone and with the network."""
+    import torch
+    from butterfly_gb300 import learned as L
+    k = 200.0
+
+    def build(seed):
+        pts, nrm, w, off, _ = B.scattering_geometry(num=64, k=k, ppw=12.0, rmin=0.05,
+                                                    rmax=0.15, box=2.0, gap=0.05, seed=seed)
+        helm = B.Helm2(k, B.LayerPot.CombinedField, alpha=-1j * k, beta=1.0)
+        fac = B.FacHelm2.make_multilevel(helm, B.Quadtree(pts, nrm, leaf_size=64),
+                                         B.Quadtree(pts, leaf_size=64), rank_eps=1e-10,
+                                         pinv_tol=1e-10, context=ctx)
+        system = B.System(fac, pts, nrm, w, off, kr_order=6, diag_shift=0.5)
+        system.build_block_jacobi()
+        system.set_apply_precision("df64")
+        return pts, system
+
+    def rhs(pts, th):
+        return torch.from_numpy(-np.exp(1j * k * (pts @ np.array([np.cos(th), np.sin(th)])))).cuda()
+
+    net = L.Mlp(4 * chunk, 256, 2 * chunk, seed=11, context=ctx)
+    rng = B.Rng(5)
+    t0 = time.perf_counter()
+    Fs, Ts = [], []
+    for seed in range(1, 1 + train_layouts):
+        pts, system = build(seed)
+        L.set_learned(system, net, chunk)
+        for th in 2 * np.pi * rng.uniform(angles):
+            F, T, _ = L.collect_pairs(system, rhs(pts, th), iterates=iterates)
+            Fs.append(F)
+            Ts.append(T)
+    F, T = torch.cat(Fs), torch.cat(Ts)
+    data_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    losses = L.train(net, F, T, epochs=epochs, batch=1024, lr=1e-3)
+    train_s = time.perf_counter() - t0
+    evals = []
+    for seed in (0, 7):
+        pts, system = build(seed)
+        L.set_learned(system, net, chunk)
+        for th in (0.4, 3.9):
+            b = rhs(pts, th)
+            row = {"layout": seed, "angle": th}
+            for pc in ("block_jacobi", "learned"):
+                B.solve_gmres(system, b, tol=1e-8, max_num_iter=3000, precond=pc)   # warm
+                torch.cuda.synchronize()
+                t = time.perf_counter()
+                _, info = B.solve_gmres(system, b, tol=1e-8, max_num_iter=3000, precond=pc)
+                torch.cuda.synchronize()
+                row[pc] = {"iterations": int(info["iterations"]), "time_s": time.perf_counter() - t,
+                           "true_rel_residual": float(info["trueRelResidual"])}
+            evals.append(row)
+    return {"network": "%d-256-256-%d ReLU, FP32" % (4 * chunk, 2 * chunk),
+            "training_pairs": int(F.shape[0]), "training_solves": train_layouts * angles,
+            "pair_collection_s": data_s, "train_s": train_s,
+            "loss_first_last_epoch": [losses[0], losses[-1]],
+            "target_mean_square": float(T.pow(2).mean().item()), "eval": evals}
+
+
 # ---------------------------------------------------------------------------
 # CPU legs (the only place bench.py runs the oracle)
 # ---------------------------------------------------------------------------
@@ -632,6 +700,11 @@ def main():
             gm = gmres_scattering(B, ctx)
         except Exception as exc:       # reported, the apply line still stands
             gm = {"error": str(exc)[:200]}
+        if args.learned:
+            try:
+                gm["learned"] = learned_scattering(B, ctx)
+            except Exception as exc:
+                gm["learned"] = {"error": str(exc)[:200]}
     launches = len(fac.launch_info()) * args.steps
     line = {"metric": METRIC, "value": rhs_s[head], "unit": "RHS/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,

@@ -633,7 +633,7 @@ class _GmresResultC(ctypes.Structure):
                 ("converged", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
-PRECOND = {"none": 0, "block_jacobi": 1, "user": 2}
+PRECOND = {"none": 0, "block_jacobi": 1, "user": 2, "learned": 3}
 _PRECOND_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                ctypes.c_void_p)
 
@@ -801,3 +801,6 @@ def scattering_geometry(num: int = 64, k: float = 200.0, ppw: float = 12.0,
         off.append(off[-1] + n)
     return (np.concatenate(pts), np.concatenate(nrm), np.concatenate(wts),
             np.array(off, dtype=np.int64), np.array(circles))
+
+
+from . import learned  # noqa: E402,F401  (learned preconditioner)

@@ -308,6 +308,99 @@ __global__ void blockDiagApply32Kernel(int64_t n, int64_t const *curveOf, int64_
   if (lane == 0) z[row] = make_double2(sr, si);
 }
 
+// Learned preconditioner, one CTA per chunk c (start, len <= chunk points).
+// The chunk is brought to a canonical scale and phase: s = ||r_c|| and
+// p = rho / |rho| with rho = sum_t |r_t| r_t, so that the preconditioner
+// commutes with every complex scaling of r (a Krylov method's vectors carry
+// arbitrary phases).  scale[3c .. 3c+2] = (s, Re p, Im p); features_c =
+// conj(p) (r_c, zbj_c) / s as (re, im) pairs, zero-padded to `chunk` points.
+__global__ void learnedFeaturesKernel(int chunk, int64_t const *start, int32_t const *len,
+                                      double2 const *r, double2 const *zbj, float *feat,
+                                      float *scale) {
+  __shared__ double red[3][32];
+  __shared__ double2 rot;   // conj(p) / s
+  int64_t const c = blockIdx.x, a = start[c];
+  int const L = len[c];
+  double q = 0, ux = 0, uy = 0;
+  for (int t = threadIdx.x; t < L; t += blockDim.x) {
+    double2 const v = r[a + t];
+    double const m2 = v.x * v.x + v.y * v.y, m = sqrt(m2);
+    q += m2;
+    ux += m * v.x;
+    uy += m * v.y;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    q += __shfl_xor_sync(0xffffffffu, q, o);
+    ux += __shfl_xor_sync(0xffffffffu, ux, o);
+    uy += __shfl_xor_sync(0xffffffffu, uy, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = q;
+    red[1][threadIdx.x >> 5] = ux;
+    red[2][threadIdx.x >> 5] = uy;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0, x = 0, y = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      t += red[0][w];
+      x += red[1][w];
+      y += red[2][w];
+    }
+    double const sN = sqrt(t), rm = sqrt(x * x + y * y);
+    double px = 1, py = 0;
+    if (rm > 0) {
+      px = x / rm;
+      py = y / rm;
+    }
+    scale[3 * c] = (float)sN;
+    scale[3 * c + 1] = (float)px;
+    scale[3 * c + 2] = (float)py;
+    double const inv = sN > 0 ? 1.0 / sN : 0.0;
+    rot = make_double2(px * inv, -py * inv);
+  }
+  __syncthreads();
+  double2 const w = rot;
+  float *f = feat + c * 4 * (int64_t)chunk;
+  for (int t = threadIdx.x; t < chunk; t += blockDim.x) {
+    double2 const rv = t < L ? r[a + t] : make_double2(0, 0);
+    double2 const zv = t < L ? zbj[a + t] : make_double2(0, 0);
+    f[2 * t] = (float)(rv.x * w.x - rv.y * w.y);
+    f[2 * t + 1] = (float)(rv.x * w.y + rv.y * w.x);
+    f[2 * chunk + 2 * t] = (float)(zv.x * w.x - zv.y * w.y);
+    f[2 * chunk + 2 * t + 1] = (float)(zv.x * w.y + zv.y * w.x);
+  }
+}
+// targets_c = conj(p) (e_c - zbj_c) / s
+__global__ void learnedTargetsKernel(int chunk, int64_t const *start, int32_t const *len,
+                                     double2 const *e, double2 const *zbj, float const *scale,
+                                     float *tgt) {
+  int64_t const c = blockIdx.x, a = start[c];
+  int const L = len[c];
+  double const sN = scale[3 * c];
+  double const inv = sN > 0 ? 1.0 / sN : 0.0;
+  double const wx = scale[3 * c + 1] * inv, wy = -scale[3 * c + 2] * inv;
+  float *t0 = tgt + c * 2 * (int64_t)chunk;
+  for (int t = threadIdx.x; t < chunk; t += blockDim.x) {
+    double2 const d = t < L ? make_double2(e[a + t].x - zbj[a + t].x, e[a + t].y - zbj[a + t].y)
+                            : make_double2(0, 0);
+    t0[2 * t] = (float)(d.x * wx - d.y * wy);
+    t0[2 * t + 1] = (float)(d.x * wy + d.y * wx);
+  }
+}
+// z_c += s p out_c
+__global__ void learnedApplyKernel(int chunk, int64_t const *start, int32_t const *len,
+                                   float const *out, float const *scale, double2 *z) {
+  int64_t const c = blockIdx.x, a = start[c];
+  int const L = len[c];
+  double const sN = scale[3 * c], px = scale[3 * c + 1] * sN, py = scale[3 * c + 2] * sN;
+  float const *o = out + c * 2 * (int64_t)chunk;
+  for (int t = threadIdx.x; t < L; t += blockDim.x) {
+    double const ox = o[2 * t], oy = o[2 * t + 1];
+    z[a + t] = make_double2(z[a + t].x + px * ox - py * oy, z[a + t].y + px * oy + py * ox);
+  }
+}
+
 __global__ void c128ToC64FlatKernel(int64_t n, double2 const *a, float2 *b) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -474,6 +567,11 @@ struct bfgSystem_s {
   bool haveBj = false;
   std::vector<int64_t> blkOff;
   Dev dBlkOff, dInv, dInv32, dWork, dColBuf, dFlag;
+  // learned preconditioner: chunks of consecutive points of a curve
+  bfgMlp mlp = nullptr;
+  int32_t chunk = 0;
+  int64_t nChunks = 0;
+  Dev dChunkStart, dChunkLen, dFeat, dOut, dScale, dZbj;
   std::string err;
   cudaStream_t stream() const;
 };
@@ -685,6 +783,72 @@ bfgStatus bfgSystemApplyBlockJacobi(bfgSystem sys, void const *R, void *Z) {
   return BFG_OK;
 }
 
+namespace {
+// z = M_bj r from the FP32 inverses
+void applyBj32(bfgSystem sys, double2 const *r, double2 *z, cudaStream_t s) {
+  int64_t const n = sys->n;
+  blockDiagApply32Kernel<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(
+      n, sys->dCurveOf.as<int64_t>(), sys->dOffsets.as<int64_t>(), sys->dBlkOff.as<int64_t>(),
+      sys->dInv32.as<float2>(), r, z);
+}
+}  // namespace
+
+bfgStatus bfgSystemSetLearnedPreconditioner(bfgSystem sys, bfgMlp mlp, int32_t chunk) {
+  if (!sys || !mlp || chunk < 1) return BFG_ERROR_INVALID_ARGUMENTS;
+  if (!sys->haveBj) return sysFail(sys, BFG_ERROR_INVALID_ARGUMENTS, "learned: block-Jacobi not built");
+  int32_t nIn = 0, nHid = 0, nOut = 0;
+  bfgMlpGetShape(mlp, &nIn, &nHid, &nOut);
+  if (nIn != 4 * chunk || nOut != 2 * chunk)
+    return sysFail(sys, BFG_ERROR_INVALID_ARGUMENTS, "learned: network shape does not fit the chunk");
+  std::vector<int64_t> st;
+  std::vector<int32_t> ln;
+  for (int64_t b = 0; b < sys->numCurves; ++b)
+    for (int64_t a = sys->offsets[b]; a < sys->offsets[b + 1]; a += chunk) {
+      st.push_back(a);
+      ln.push_back((int32_t)std::min<int64_t>(chunk, sys->offsets[b + 1] - a));
+    }
+  cudaStream_t s = sys->stream();
+  int64_t const nc = (int64_t)st.size();
+  SYS_CK(sys->dChunkStart.alloc(std::max<int64_t>(1, nc) * 8));
+  SYS_CK(sys->dChunkLen.alloc(std::max<int64_t>(1, nc) * 4));
+  SYS_CK(sys->dFeat.alloc(std::max<int64_t>(1, nc) * 4 * chunk * 4));
+  SYS_CK(sys->dOut.alloc(std::max<int64_t>(1, nc) * 2 * chunk * 4));
+  SYS_CK(sys->dScale.alloc(std::max<int64_t>(1, nc) * 3 * 4));
+  SYS_CK(sys->dZbj.alloc(sys->n * 16));
+  SYS_CK(cudaMemcpyAsync(sys->dChunkStart.p, st.data(), nc * 8, cudaMemcpyHostToDevice, s));
+  SYS_CK(cudaMemcpyAsync(sys->dChunkLen.p, ln.data(), nc * 4, cudaMemcpyHostToDevice, s));
+  SYS_CK(cudaStreamSynchronize(s));
+  sys->mlp = mlp;
+  sys->chunk = chunk;
+  sys->nChunks = nc;
+  return BFG_OK;
+}
+
+bfgStatus bfgSystemLearnedNumChunks(bfgSystem sys, int64_t *numChunks) {
+  if (!sys || !numChunks) return BFG_ERROR_INVALID_ARGUMENTS;
+  *numChunks = sys->nChunks;
+  return BFG_OK;
+}
+
+bfgStatus bfgSystemLearnedPairs(bfgSystem sys, void const *R, void const *E, void *features,
+                                void *targets) {
+  if (!sys || !R || !features || (E && !targets)) return BFG_ERROR_INVALID_ARGUMENTS;
+  if (!sys->chunk) return sysFail(sys, BFG_ERROR_INVALID_ARGUMENTS, "learned: no chunks set");
+  cudaStream_t s = sys->stream();
+  double2 const *r = static_cast<double2 const *>(R);
+  double2 *zbj = sys->dZbj.as<double2>();
+  applyBj32(sys, r, zbj, s);
+  learnedFeaturesKernel<<<(unsigned)sys->nChunks, 128, 0, s>>>(
+      sys->chunk, sys->dChunkStart.as<int64_t>(), sys->dChunkLen.as<int32_t>(), r, zbj,
+      static_cast<float *>(features), sys->dScale.as<float>());
+  if (E)
+    learnedTargetsKernel<<<(unsigned)sys->nChunks, 128, 0, s>>>(
+        sys->chunk, sys->dChunkStart.as<int64_t>(), sys->dChunkLen.as<int32_t>(),
+        static_cast<double2 const *>(E), zbj, sys->dScale.as<float>(), static_cast<float *>(targets));
+  SYS_CK(cudaGetLastError());
+  return BFG_OK;
+}
+
 bfgStatus bfgSolveGmres(bfgSystem sys, void const *B, void *X, double tol, int64_t maxIter,
                         int32_t precond, bfgPrecondFn userFn, void *userData,
                         bfgGmresResult *result) {
@@ -693,7 +857,10 @@ bfgStatus bfgSolveGmres(bfgSystem sys, void const *B, void *X, double tol, int64
     return sysFail(sys, BFG_ERROR_INVALID_ARGUMENTS, "block-Jacobi not built");
   if (precond == BFG_PRECOND_USER && !userFn)
     return sysFail(sys, BFG_ERROR_INVALID_ARGUMENTS, "user preconditioner missing");
-  if (precond != BFG_PRECOND_NONE && precond != BFG_PRECOND_BLOCK_JACOBI && precond != BFG_PRECOND_USER)
+  if (precond == BFG_PRECOND_LEARNED && !sys->mlp)
+    return sysFail(sys, BFG_ERROR_INVALID_ARGUMENTS, "learned preconditioner not set");
+  if (precond != BFG_PRECOND_NONE && precond != BFG_PRECOND_BLOCK_JACOBI &&
+      precond != BFG_PRECOND_USER && precond != BFG_PRECOND_LEARNED)
     return sysFail(sys, BFG_ERROR_INVALID_ARGUMENTS, "unknown preconditioner");
   auto t0 = std::chrono::steady_clock::now();
   cudaStream_t s = sys->stream();
@@ -738,9 +905,21 @@ bfgStatus bfgSolveGmres(bfgSystem sys, void const *B, void *X, double tol, int64
       return BFG_OK;
     }
     if (precond == BFG_PRECOND_BLOCK_JACOBI) {
-      blockDiagApply32Kernel<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(
-          n, sys->dCurveOf.as<int64_t>(), sys->dOffsets.as<int64_t>(),
-          sys->dBlkOff.as<int64_t>(), sys->dInv32.as<float2>(), in, outv);
+      applyBj32(sys, in, outv, s);
+      SYS_CK(cudaGetLastError());
+      return BFG_OK;
+    }
+    if (precond == BFG_PRECOND_LEARNED) {
+      applyBj32(sys, in, outv, s);
+      int64_t const *cs = sys->dChunkStart.as<int64_t>();
+      int32_t const *cl = sys->dChunkLen.as<int32_t>();
+      learnedFeaturesKernel<<<(unsigned)sys->nChunks, 128, 0, s>>>(
+          sys->chunk, cs, cl, in, outv, sys->dFeat.as<float>(), sys->dScale.as<float>());
+      SYS_CK(cudaGetLastError());
+      bfgStatus ms = bfgMlpForward(sys->mlp, sys->dFeat.p, sys->nChunks, sys->dOut.p);
+      if (ms != BFG_OK) return sysFail(sys, ms, "learned preconditioner: network failed");
+      learnedApplyKernel<<<(unsigned)sys->nChunks, 128, 0, s>>>(
+          sys->chunk, cs, cl, sys->dOut.as<float>(), sys->dScale.as<float>(), outv);
       SYS_CK(cudaGetLastError());
       return BFG_OK;
     }

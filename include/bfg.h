@@ -287,6 +287,52 @@ bfgStatus bfgSystemApplyBlockJacobi(bfgSystem sys, void const *R, void *Z);
 #define BFG_PRECOND_NONE 0
 #define BFG_PRECOND_BLOCK_JACOBI 1
 #define BFG_PRECOND_USER 2
+#define BFG_PRECOND_LEARNED 3
+
+/* ---- Learned preconditioner (a GB300 addition; the reference
+ * preconditions with block-Jacobi only) ---- */
+typedef struct bfgMlp_s *bfgMlp;
+/* A perceptron nIn -> nHidden -> nHidden -> nOut with ReLU between the
+ * layers, FP32 parameters on the context's GPU, He-uniform weights from
+ * `seed` (the output layer scaled by 0.1) and zero biases.  Forward,
+ * gradients and Adam run in hand-written kernels, in a fixed order (the
+ * same batch gives the same gradients bit for bit). */
+bfgStatus bfgMlpCreate(bfgContext ctx, int32_t nIn, int32_t nHidden, int32_t nOut,
+                       uint64_t seed, bfgMlp *mlp);
+bfgStatus bfgMlpDestroy(bfgMlp mlp);
+bfgStatus bfgMlpGetShape(bfgMlp mlp, int32_t *nIn, int32_t *nHidden, int32_t *nOut);
+/* The parameters as one FP32 array: W1 (nIn x nHidden, row-major), b1, W2
+ * (nHidden x nHidden), b2, W3 (nHidden x nOut), b3.  Get/Set copy to/from
+ * the host; Set also resets the optimiser. */
+bfgStatus bfgMlpNumParams(bfgMlp mlp, int64_t *count);
+bfgStatus bfgMlpGetParams(bfgMlp mlp, float *params);
+bfgStatus bfgMlpSetParams(bfgMlp mlp, float const *params);
+/* Y (batch x nOut) = network(X (batch x nIn)); device FP32, row-major. */
+bfgStatus bfgMlpForward(bfgMlp mlp, void const *X, int64_t batch, void *Y);
+/* The loss mean_b 0.5 ||y_b - t_b||^2 of one batch (device X, T) and its
+ * gradient (host, parameter layout; may be NULL); no update. */
+bfgStatus bfgMlpGradients(bfgMlp mlp, void const *X, void const *T, int64_t batch,
+                          float *grad, double *loss);
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8, learning rate lr) on one
+ * batch; *loss = the loss before the step. */
+bfgStatus bfgMlpTrainStep(bfgMlp mlp, void const *X, void const *T, int64_t batch, float lr,
+                          double *loss);
+
+/* BFG_PRECOND_LEARNED: z = M_bj r + s_c p_c mlp(features_c) on every chunk
+ * c of `chunk` consecutive points of a curve, with M_bj the block-Jacobi
+ * preconditioner (FP32 copy), s_c = ||r_c||, p_c the phase of sum_t |r_t|
+ * r_t over the chunk and features_c = conj(p_c) (r_c, (M_bj r)_c) / s_c as
+ * interleaved (re, im) pairs, zero-padded to `chunk` points (nIn = 4 chunk,
+ * nOut = 2 chunk): the preconditioner commutes with complex scalings of r.  Requires the block-Jacobi inverses; `mlp`
+ * must live as long as it is used. */
+bfgStatus bfgSystemSetLearnedPreconditioner(bfgSystem sys, bfgMlp mlp, int32_t chunk);
+bfgStatus bfgSystemLearnedNumChunks(bfgSystem sys, int64_t *numChunks);
+/* Training pairs: for a residual R and its exact correction E = A^-1 R
+ * (device complex128; E may be NULL), the chunk features (numChunks x 4
+ * chunk) and targets conj(p_c) (E - M_bj R)_c / s_c (numChunks x 2 chunk),
+ * device FP32. */
+bfgStatus bfgSystemLearnedPairs(bfgSystem sys, void const *R, void const *E, void *features,
+                                void *targets);
 /* A right preconditioner z = M r on device complex128 vectors, launched on
  * `cudaStream`; may change from call to call (flexible GMRES). */
 typedef bfgStatus (*bfgPrecondFn)(void *userData, void const *r, void *z, void *cudaStream);
