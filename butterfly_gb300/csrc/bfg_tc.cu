@@ -58,8 +58,9 @@ struct TcLayout {
   // past a short tile (rows whose outputs are discarded): 2 KB of slack
   // follow the last stage
   static constexpr int barOff = kTcStages * stageBytes + 2048;
-  // fullA[S], fullB[S], empty[S], accFull[2], accEmpty[2], TMEM slot, abort
-  static constexpr int smemBytes = barOff + 8 * (3 * kTcStages + 4) + 16;
+  // fullA[S], fullB[S], empty[S], accFull[2], accEmpty[2], fullX[S], TMEM
+  // slot, abort
+  static constexpr int smemBytes = barOff + 8 * (4 * kTcStages + 4) + 16;
   static_assert(smemBytes <= 232448, "shared memory per CTA");
   static_assert(kTcStages % 2 == 0, "stages must hold one chunk parity each");
 };
@@ -252,10 +253,10 @@ __global__ void __launch_bounds__(256) tcFillKernel(TcFill const *__restrict__ f
 
 // Persistent CTA over its chunk stream (one apply stage, one tile of 16 RHS),
 // warp-specialised around mbarriers:
-//   warp 8           bulk-copies the A planes of chunk i into stage i % 4
-//                    once the MMAs of chunk i-4 are done (empty), and with
-//                    them (fullA) the chunk's FP32 right-hand-side rows when
-//                    they form one aligned block;
+//   warp 8           once the MMAs of chunk i-4 are done (empty) bulk-copies
+//                    chunk i's FP32 right-hand-side rows when they form one
+//                    aligned block (fullX), then its A planes into stage
+//                    i % 4 (fullA);
 //   warps 0-3        otherwise copy chunk i+2's right-hand sides into its
 //                    stage (cp.async); build chunk i's bf16 B planes (fullB);
 //   warps 9, 10      (lane 0) issue the MMAs of the even and the odd chunks,
@@ -297,12 +298,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
   uint32_t const sbase = smemAddr(smem);
   uint32_t const fullA = sbase + L::barOff, fullB = fullA + 8 * S, empty = fullB + 8 * S;
   uint32_t const accFull = empty + 8 * S, accEmpty = accFull + 16;
-  uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(smem + L::barOff + 8 * (3 * S + 4));
+  uint32_t const fullX = accEmpty + 16;
+  uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(smem + L::barOff + 8 * (4 * S + 4));
   int volatile *abortFlag = reinterpret_cast<int volatile *>(tmemSlot + 1);
 
   if (tid == 0) {
     for (int s = 0; s < S; ++s) {
       mbarInit(fullA + 8 * s, 1);
+      mbarInit(fullX + 8 * s, 1);
       mbarInit(fullB + 8 * s, kBuilders / 32);
       mbarInit(empty + 8 * s, 1);
     }
@@ -347,17 +350,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
       }
       bool const bulk = inIsX ? bulkX : bulkW;
       if (lane == 0) {
-        mbarExpectTx(fullA + 8 * s, plane * TERMS + (bulk ? (uint32_t)nc * 128 : 0u));
+        // the input rows first, on their own barrier (every chunk arrives on
+        // it, with no bytes on the cp.async path, so its phases follow the
+        // chunks): the builders convert them while the A planes stream in
+        mbarExpectTx(fullX + 8 * s, bulk ? (uint32_t)nc * 128 : 0u);
+        // the chunk's input rows are one contiguous block (leading dimension 16)
+        if (bulk)
+          bulkG2S(sbase + s * L::stageBytes + L::aBytes + L::bBytes,
+                  (inIsX ? X : W) + inRow * kTcRhs, (uint32_t)nc * (kTcRhs * 8), fullX + 8 * s);
+        mbarExpectTx(fullA + 8 * s, plane * TERMS);
 #pragma unroll
         for (int t = 0; t < TERMS; ++t)
           bulkG2S(sbase + s * L::stageBytes + t * kAPlaneBytes, tarena + off + (int64_t)t * plane,
                   plane, fullA + 8 * s);
       }
       __syncwarp();
-      // the chunk's input rows are one contiguous block (leading dimension 16)
-      if (bulk && lane == 0)
-        bulkG2S(sbase + s * L::stageBytes + L::aBytes + L::bBytes,
-                (inIsX ? X : W) + inRow * kTcRhs, (uint32_t)nc * (kTcRhs * 8), fullA + 8 * s);
       issued = i + 1;
       off = offN;
       inRow = inRowN;
@@ -366,8 +373,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
       inIsX = inIsXN;
     }
     if (lane == 0 && *abortFlag)   // copies still in flight land before the CTA exits
-      for (int64_t j = issued > S ? issued - S : 0; j < issued; ++j)
+      for (int64_t j = issued > S ? issued - S : 0; j < issued; ++j) {
+        mbarDrain(fullX + 8 * (j % S), (uint32_t)((j / S) & 1));
         mbarDrain(fullA + 8 * (j % S), (uint32_t)((j / S) & 1));
+      }
   } else if (warp == kMmaWarp || warp == kMmaWarp + 1) {
     // ---- MMAs: warp kMmaWarp issues the even chunks, the next warp the odd
     // ones, so one thread's waits and bookkeeping overlap the other's MMAs in
@@ -486,10 +495,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
         // chunk i+2-S, which this thread has converted
         if (i + 2 < nCh && !bulkOf(d2)) issueX(d2, i + 2);
         cpAsyncCommit();
-        // bulk inputs land with the A planes, which the producer copies only
-        // once the MMAs of chunk i-S are done; the empty wait then returns
-        // at once
-        if (bulkOf(d0) && !mbarWait(fullA + 8 * s, (uint32_t)((i / S) & 1), abortFlag)) {
+        // bulk inputs land on fullX, which the producer arrives on only once
+        // the MMAs of chunk i-S are done; the empty wait then returns at once
+        if (bulkOf(d0) && !mbarWait(fullX + 8 * s, (uint32_t)((i / S) & 1), abortFlag)) {
           *abortFlag = 1;
           break;
         }
