@@ -113,6 +113,8 @@ def lib() -> ctypes.CDLL:
         "bfgFacCopyBlocks": [_VP, _VP, _I64, _VP, _I64],
         "bfgFacApply": [_VP, ctypes.c_int, _VP, _I64, _I64, _VP, _I64, ctypes.c_uint32],
         "bfgFacApplyHost": [_VP, ctypes.c_int, _VP, _I64, _I64, _VP, _I64, ctypes.c_uint32],
+        "bfgFacApplyHostAsync": [_VP, ctypes.c_int, _VP, _I64, _I64, _VP, _I64, ctypes.c_uint32],
+        "bfgFacApplyHostWait": [_VP],
         "bfgFacApplyTimed": [_VP, ctypes.c_int, _VP, _I64, _I64, _VP, _I64, ctypes.c_uint32,
                              _VP, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)],
         "bfgFacDenseRows": [_VP, _VP, _I64, _VP, _I64, _I64, _VP, _I64],

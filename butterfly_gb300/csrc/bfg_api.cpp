@@ -82,6 +82,25 @@ struct bfgFac_s {
   DevBuf items, contribs, rowSeg, segStart, segContrib0, segBase;
   DevBuf ws, xbuf;
   DevBuf hx128, hy128, hx64, hy64;  // staging of the host-operand apply
+  // pipelined host-operand applies (bfgFacApplyHostAsync): two staging
+  // slots; uploads and downloads on streams of their own, so that one
+  // call's copies overlap another's compute on the context's stream
+  struct HostSlot {
+    DevBuf x128, y128, x64, y64;
+    cudaEvent_t uploaded = nullptr, consumed = nullptr, computed = nullptr, downloaded = nullptr;
+    bool started = false;
+  } hslot[2];
+  cudaStream_t upStream = nullptr, downStream = nullptr;
+  int64_t asyncCalls = 0;
+  ~bfgFac_s() {
+    if (upStream) cudaStreamSynchronize(upStream);
+    if (downStream) cudaStreamSynchronize(downStream);
+    for (auto &h : hslot)
+      for (cudaEvent_t e : {h.uploaded, h.consumed, h.computed, h.downloaded})
+        if (e) cudaEventDestroy(e);
+    if (upStream) cudaStreamDestroy(upStream);
+    if (downStream) cudaStreamDestroy(downStream);
+  }
   std::vector<int64_t> stageItem0;
   // split-BF16 tensor-core apply, per plane count (index terms - 2): the
   // chunk schedule of the 128-row program and the bf16 planes of the factors
@@ -1227,9 +1246,14 @@ bfgStatus bfgFacApplyHost(bfgFac f, bfgPrecision prec, double const *X, int64_t 
     // whatever the arithmetic); the buffers persist across calls
     ck(f->hx128.ensure((size_t)nc * R * 16), "apply buffers");
     ck(f->hy128.ensure((size_t)nr * R * 16), "apply buffers");
-    ck(cudaMemcpy2DAsync(f->hx128.p, (size_t)R * 16, X, (size_t)ldx * 16, (size_t)R * 16,
-                         (size_t)nc, cudaMemcpyHostToDevice, s),
-       "copy X");
+    // one contiguous copy when the rows are back to back (a 2D copy of
+    // 256-byte rows moves them one by one)
+    if (ldx == R)
+      ck(cudaMemcpyAsync(f->hx128.p, X, (size_t)nc * R * 16, cudaMemcpyHostToDevice, s), "copy X");
+    else
+      ck(cudaMemcpy2DAsync(f->hx128.p, (size_t)R * 16, X, (size_t)ldx * 16, (size_t)R * 16,
+                           (size_t)nc, cudaMemcpyHostToDevice, s),
+         "copy X");
     if (prec == BFG_PRECISION_FP64 || prec == BFG_PRECISION_DF64) {
       bfgStatus st = applyDispatch(f, prec, f->hx128.p, R, R, f->hy128.p, R, flags, nullptr);
       if (st != BFG_OK) return st;
@@ -1245,9 +1269,12 @@ bfgStatus bfgFacApplyHost(bfgFac f, bfgPrecision prec, double const *X, int64_t 
     } else {
       return fail(f->ctx, BFG_ERROR_NOT_IMPLEMENTED, "apply: unknown precision");
     }
-    ck(cudaMemcpy2DAsync(Y, (size_t)ldy * 16, f->hy128.p, (size_t)R * 16, (size_t)R * 16,
-                         (size_t)nr, cudaMemcpyDeviceToHost, s),
-       "copy Y");
+    if (ldy == R)
+      ck(cudaMemcpyAsync(Y, f->hy128.p, (size_t)nr * R * 16, cudaMemcpyDeviceToHost, s), "copy Y");
+    else
+      ck(cudaMemcpy2DAsync(Y, (size_t)ldy * 16, f->hy128.p, (size_t)R * 16, (size_t)R * 16,
+                           (size_t)nr, cudaMemcpyDeviceToHost, s),
+         "copy Y");
     ck(cudaStreamSynchronize(s), "apply");
     if (isTcPrecision(prec)) checkTcStatus(f);
     return BFG_OK;
@@ -1261,6 +1288,86 @@ bfgStatus bfgFacPrepare(bfgFac f, bfgPrecision prec) {
   return guarded(f->ctx, [&]() -> bfgStatus {
     preparePrecision(f, prec);
     ck(cudaStreamSynchronize(f->ctx->stream), "prepare");
+    return BFG_OK;
+  });
+}
+
+bfgStatus bfgFacApplyHostAsync(bfgFac f, bfgPrecision prec, double const *X, int64_t ldx,
+                               int64_t R, double *Y, int64_t ldy, uint32_t flags) {
+  if (!f) return BFG_ERROR_INVALID_ARGUMENTS;
+  return guarded(f->ctx, [&]() -> bfgStatus {
+    if (!X || !Y || R < 1 || ldx < R || ldy < R)
+      return fail(f->ctx, BFG_ERROR_INVALID_ARGUMENTS, "apply: bad operand pointers or shapes");
+    bool const c128 = prec == BFG_PRECISION_FP64 || prec == BFG_PRECISION_DF64;
+    if (!c128 && prec != BFG_PRECISION_FP32 && !isTcPrecision(prec))
+      return fail(f->ctx, BFG_ERROR_NOT_IMPLEMENTED, "apply: unknown precision");
+    preparePrecision(f, prec);
+    if (!f->upStream) {
+      ck(cudaStreamCreateWithFlags(&f->upStream, cudaStreamNonBlocking), "copy streams");
+      ck(cudaStreamCreateWithFlags(&f->downStream, cudaStreamNonBlocking), "copy streams");
+      for (auto &h : f->hslot)
+        for (cudaEvent_t *e : {&h.uploaded, &h.consumed, &h.computed, &h.downloaded})
+          ck(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "copy events");
+    }
+    cudaStream_t const cs = f->ctx->stream, up = f->upStream, down = f->downStream;
+    int64_t const nr = f->prog.numRows, nc = f->prog.numCols;
+    auto &h = f->hslot[f->asyncCalls & 1];
+    ck(h.x128.ensure((size_t)nc * R * 16), "apply buffers");
+    ck(h.y128.ensure((size_t)nr * R * 16), "apply buffers");
+    if (!c128) {
+      ck(h.x64.ensure((size_t)nc * R * 8), "apply buffers");
+      ck(h.y64.ensure((size_t)nr * R * 8), "apply buffers");
+    }
+    // upload, once the compute of this slot's previous call has read it
+    if (h.started) ck(cudaStreamWaitEvent(up, h.consumed, 0), "order");
+    if (ldx == R)
+      ck(cudaMemcpyAsync(h.x128.p, X, (size_t)nc * R * 16, cudaMemcpyHostToDevice, up), "copy X");
+    else
+      ck(cudaMemcpy2DAsync(h.x128.p, (size_t)R * 16, X, (size_t)ldx * 16, (size_t)R * 16,
+                           (size_t)nc, cudaMemcpyHostToDevice, up),
+         "copy X");
+    ck(cudaEventRecord(h.uploaded, up), "order");
+    // compute, once the upload landed and the slot's previous download left
+    ck(cudaStreamWaitEvent(cs, h.uploaded, 0), "order");
+    if (h.started) ck(cudaStreamWaitEvent(cs, h.downloaded, 0), "order");
+    if (c128) {
+      bfgStatus st = applyDispatch(f, prec, h.x128.p, R, R, h.y128.p, R, flags, nullptr);
+      if (st != BFG_OK) return st;
+      ck(cudaEventRecord(h.consumed, cs), "order");
+    } else {
+      ck(bfg::launchC128ToC64(h.x128.as<double2>(), R, nc, R, h.x64.as<float2>(), R, cs),
+         "convert X");
+      ck(cudaEventRecord(h.consumed, cs), "order");
+      bfgStatus st = applyDispatch(f, prec, h.x64.p, R, R, h.y64.p, R, flags, nullptr);
+      if (st != BFG_OK) return st;
+      ck(bfg::launchC64ToC128(h.y64.as<float2>(), R, nr, R, h.y128.as<double2>(), R, cs),
+         "convert Y");
+    }
+    ck(cudaEventRecord(h.computed, cs), "order");
+    // download
+    ck(cudaStreamWaitEvent(down, h.computed, 0), "order");
+    if (ldy == R)
+      ck(cudaMemcpyAsync(Y, h.y128.p, (size_t)nr * R * 16, cudaMemcpyDeviceToHost, down), "copy Y");
+    else
+      ck(cudaMemcpy2DAsync(Y, (size_t)ldy * 16, h.y128.p, (size_t)R * 16, (size_t)R * 16,
+                           (size_t)nr, cudaMemcpyDeviceToHost, down),
+         "copy Y");
+    ck(cudaEventRecord(h.downloaded, down), "order");
+    h.started = true;
+    ++f->asyncCalls;
+    return BFG_OK;
+  });
+}
+
+bfgStatus bfgFacApplyHostWait(bfgFac f) {
+  if (!f) return BFG_ERROR_INVALID_ARGUMENTS;
+  return guarded(f->ctx, [&]() -> bfgStatus {
+    if (f->upStream) {
+      ck(cudaStreamSynchronize(f->upStream), "apply");
+      ck(cudaStreamSynchronize(f->downStream), "apply");
+    }
+    ck(cudaStreamSynchronize(f->ctx->stream), "apply");
+    checkTcStatus(f);
     return BFG_OK;
   });
 }

@@ -202,6 +202,17 @@ bfgStatus bfgFacApply(bfgFac fac, bfgPrecision precision, void const *X, int64_t
 bfgStatus bfgFacApplyHost(bfgFac fac, bfgPrecision precision, double const *X,
                           int64_t ldx, int64_t numRhs, double *Y, int64_t ldy,
                           uint32_t flags);
+/* The same, enqueued: returns at once, the copies run on streams of their
+ * own so that one call's upload and download overlap another call's
+ * compute (two calls in flight per factorization; a third waits on the
+ * device for the first).  X must stay unchanged and Y unread until
+ * bfgFacApplyHostWait returns; X and Y should be pinned host memory
+ * (pageable memory makes the copies synchronous). */
+bfgStatus bfgFacApplyHostAsync(bfgFac fac, bfgPrecision precision, double const *X,
+                               int64_t ldx, int64_t numRhs, double *Y, int64_t ldy,
+                               uint32_t flags);
+/* Waits for every enqueued host-operand apply of the factorization. */
+bfgStatus bfgFacApplyHostWait(bfgFac fac);
 
 /* No counterpart in the reference.  The FP64 product of bfgFacApply (device
  * complex128 X and Y, same flags and contract) for callers that cannot

@@ -135,3 +135,23 @@ def test_df64_apply_is_deterministic_and_timed(ctx):
     Y = torch.empty_like(X)
     ms = fac.apply_timed(X.data_ptr(), 2, 2, Y.data_ptr(), 2, "df64")
     assert len(ms) == len(fac.launch_info())
+
+
+@pytest.mark.parametrize("prec", ["fp64", "df64", "bf16x3"])
+def test_pipelined_host_apply_matches_synchronous(ctx, prec):
+    """bfgFacApplyHostAsync: several calls in flight (two staging slots, a
+    third call waits on the device), the same results as bfgFacApplyHost."""
+    g, fac = golden_fac("star_n2048_k48", ctx)
+    lib = B.lib()
+    P = B.PRECISIONS[prec]
+    R = 4
+    Xs = [np.ascontiguousarray(O.RefRng(40 + i).complex_randn(2048 * R).reshape(2048, R))
+          for i in range(5)]
+    Xp = [torch.from_numpy(x).pin_memory() for x in Xs]
+    Yp = [torch.zeros((2048, R), dtype=torch.complex128).pin_memory() for _ in Xs]
+    for x, y in zip(Xp, Yp):
+        ctx.check(lib.bfgFacApplyHostAsync(fac.handle, P, B._VP(x.data_ptr()), R, R,
+                                           B._VP(y.data_ptr()), R, 0))
+    ctx.check(lib.bfgFacApplyHostWait(fac.handle))
+    for x, y in zip(Xs, Yp):
+        assert np.array_equal(y.numpy(), fac.apply(x, precision=prec))
