@@ -28,3 +28,12 @@ cudaError_t launchAdam(int64_t n, float *w, float const *g, float *m, float *v, 
                        float b1, float b2, float eps, int64_t step, cudaStream_t s);
 
 }  // namespace bfg
+
+struct bfgMlp_s;
+namespace bfg {
+// bfgMlpForward on the given stream (the learned preconditioner runs it on
+// its system's stream, whatever context the network was created on)
+int mlpForwardOnStream(bfgMlp_s *mlp, float const *X, int64_t batch, float *Y,
+                       cudaStream_t stream);
+
+}  // namespace bfg

@@ -61,8 +61,7 @@ namespace {
     if ((expr) != cudaSuccess) return BFG_ERROR_CUDA; \
   } while (0)
 
-bfgStatus forward(bfgMlp n, float const *X, int64_t batch, float *Y) {
-  cudaStream_t s = n->stream();
+bfgStatus forwardOn(bfgMlp n, float const *X, int64_t batch, float *Y, cudaStream_t s) {
   int const B = (int)batch;
   float const *p = n->params;
   MLP_CK(bfg::launchGemm(false, false, B, n->nHid, n->nIn, X, n->nIn, p + n->oW1, n->nHid, n->H1(),
@@ -72,6 +71,9 @@ bfgStatus forward(bfgMlp n, float const *X, int64_t batch, float *Y) {
   MLP_CK(bfg::launchGemm(false, false, B, n->nOut, n->nHid, n->H2(), n->nHid, p + n->oW3, n->nOut,
                          Y, n->nOut, p + n->ob3, bfg::kEpiNone, nullptr, 0, s));
   return BFG_OK;
+}
+bfgStatus forward(bfgMlp n, float const *X, int64_t batch, float *Y) {
+  return forwardOn(n, X, batch, Y, n->stream());
 }
 
 // gradients of mean_b 0.5 ||y_b - t_b||^2 into n->grads; loss to *loss
@@ -110,6 +112,14 @@ bfgStatus backward(bfgMlp n, float const *X, float const *T, int64_t batch, doub
 }
 
 }  // namespace
+
+int bfg::mlpForwardOnStream(bfgMlp_s *n, float const *X, int64_t batch, float *Y,
+                            cudaStream_t stream) {
+  if (!n || !X || !Y || batch < 0 || batch > (1 << 30)) return BFG_ERROR_INVALID_ARGUMENTS;
+  if (batch == 0) return BFG_OK;
+  if (!n->ensureScratch(batch)) return BFG_ERROR_MEMORY;
+  return forwardOn(n, X, batch, Y, stream);
+}
 
 extern "C" {
 

@@ -31,6 +31,7 @@
 
 #include "../../include/bfg.h"
 #include "bfg_kernels.cuh"
+#include "bfg_mlp.cuh"
 #include "hankel.cuh"
 
 namespace {
@@ -916,7 +917,8 @@ bfgStatus bfgSolveGmres(bfgSystem sys, void const *B, void *X, double tol, int64
       learnedFeaturesKernel<<<(unsigned)sys->nChunks, 128, 0, s>>>(
           sys->chunk, cs, cl, in, outv, sys->dFeat.as<float>(), sys->dScale.as<float>());
       SYS_CK(cudaGetLastError());
-      bfgStatus ms = bfgMlpForward(sys->mlp, sys->dFeat.p, sys->nChunks, sys->dOut.p);
+      bfgStatus ms = (bfgStatus)bfg::mlpForwardOnStream(sys->mlp, sys->dFeat.as<float>(),
+                                                        sys->nChunks, sys->dOut.as<float>(), s);
       if (ms != BFG_OK) return sysFail(sys, ms, "learned preconditioner: network failed");
       learnedApplyKernel<<<(unsigned)sys->nChunks, 128, 0, s>>>(
           sys->chunk, cs, cl, sys->dOut.as<float>(), sys->dScale.as<float>(), outv);

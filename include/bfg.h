@@ -334,7 +334,8 @@ bfgStatus bfgMlpTrainStep(bfgMlp mlp, void const *X, void const *T, int64_t batc
  * preconditioner (FP32 copy), s_c = ||r_c||, p_c the phase of sum_t |r_t|
  * r_t over the chunk and features_c = conj(p_c) (r_c, (M_bj r)_c) / s_c as
  * interleaved (re, im) pairs, zero-padded to `chunk` points (nIn = 4 chunk,
- * nOut = 2 chunk): the preconditioner commutes with complex scalings of r.  Requires the block-Jacobi inverses; `mlp`
+ * nOut = 2 chunk): the preconditioner commutes with complex scalings of r.
+ * The network runs on the system's stream.  Requires the block-Jacobi inverses; `mlp`
  * must live as long as it is used. */
 bfgStatus bfgSystemSetLearnedPreconditioner(bfgSystem sys, bfgMlp mlp, int32_t chunk);
 bfgStatus bfgSystemLearnedNumChunks(bfgSystem sys, int64_t *numChunks);

@@ -117,3 +117,10 @@ def test_learned_fgmres_trained_on_own_solves(scattering):
             assert info["converged"] == 1 and info["trueRelResidual"] < 1e-9
             its.setdefault(pc, []).append(info["iterations"])
     print("iterations block-Jacobi %s learned %s" % (its["block_jacobi"], its["learned"]))
+
+
+def test_learned_rejects_a_network_of_the_wrong_shape(scattering):
+    system = scattering["system"]
+    net = L.Mlp(4 * 16, 32, 2 * 8, seed=1)         # output for 8 points, chunks of 16
+    with pytest.raises(B.BfgError):
+        L.set_learned(system, net, 16)
