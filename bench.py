@@ -607,6 +607,12 @@ def main():
         Y16 = torch.empty((n, R), dtype=torch.complex64, device="cuda")
     stream.synchronize()
     # bf16x3 / bf16x2: tensor-core products of split-BF16 planes, complex64 vectors
+    # the tensor-core schedules: per stage the fastest of several CTA dealings
+    # (bfgFacAutotune), before anything is timed
+    tuned = {}
+    for p in ("bf16x3", "bf16x2"):
+        t = fac.autotune(p, R)
+        tuned[p] = {"default_ms": [float(v) for v in t[:, 0]], "tuned_ms": [float(v) for v in t[:, 1]]}
     # df64: FP64-accurate double-float arithmetic, complex128 vectors
     with torch.cuda.stream(stream):
         Ydf = torch.empty_like(Y64)
@@ -739,7 +745,7 @@ def main():
                               "max_rank": st["maxRank"],
                               "jacobi_not_converged": st["jacobiNotConverged"]},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-            "gpu_launches": launches, "gmres": gm}
+            "gpu_launches": launches, "gmres": gm, "autotune": tuned}
     print(json.dumps(line))
 
 

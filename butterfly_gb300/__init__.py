@@ -127,6 +127,8 @@ def lib() -> ctypes.CDLL:
                          _VP, _VP, ctypes.c_char_p, _I64, ctypes.POINTER(_I64)],
         "bfgBessel01Host": [_VP, _I64, _VP],
         "bfgFacPrepare": [_VP, ctypes.c_int32],
+        "bfgFacAutotune": [_VP, ctypes.c_int32, _I64, _VP, ctypes.c_int32,
+                           ctypes.POINTER(ctypes.c_int32)],
         "bfgQuadtreeBuild": [_VP, _VP, _VP, _I64, _I64, ctypes.c_int32, _VP, _VP, _I64, _VP],
         "bfgRngSeed": [ctypes.POINTER(_RngC), ctypes.c_uint64],
         "bfgRngUniform1": [ctypes.POINTER(_RngC)],
@@ -361,6 +363,15 @@ class Fac:
 
     def __del__(self):
         self.close()
+
+    def autotune(self, precision: str = "bf16x3", rhs: int = 16):
+        """bfgFacAutotune: per-stage schedules of the tensor-core apply picked
+        by timing; returns (default ms, tuned ms) per stage."""
+        out = np.zeros(64, dtype=np.float64)
+        ns = ctypes.c_int32()
+        self.ctx.check(lib().bfgFacAutotune(self.handle, PRECISIONS[precision], int(rhs),
+                                            _ptr(out), len(out), ctypes.byref(ns)), "autotune")
+        return out[:2 * ns.value].reshape(-1, 2)
 
     def prepare(self, precision: str):
         """Builds the precision's copy of the factors now (bfgFacPrepare)."""

@@ -1281,6 +1281,93 @@ bfgStatus bfgFacApplyHost(bfgFac f, bfgPrecision prec, double const *X, int64_t 
   });
 }
 
+bfgStatus bfgFacAutotune(bfgFac f, bfgPrecision prec, int64_t R, double *stageMs,
+                         int32_t capacity, int32_t *numStages) {
+  if (!f || R < 1 || (capacity > 0 && !stageMs)) return BFG_ERROR_INVALID_ARGUMENTS;
+  if (!isTcPrecision(prec))
+    return fail(f->ctx, BFG_ERROR_NOT_IMPLEMENTED,
+                "autotune: the tuned schedule is the tensor-core apply's (BF16X2, BF16X3)");
+  return guarded(f->ctx, [&]() -> bfgStatus {
+    int const terms = prec == BFG_PRECISION_BF16X3 ? 3 : 2;
+    ensureTc(f, terms);
+    bfgFac_s::Tc &tc = f->tc[terms - 2];
+    cudaStream_t s = f->ctx->stream;
+    bfg::ApplyProgram p128;
+    bfg::makeApplyProgram(f->plan, p128, bfg::kTcRows);
+    size_t const nStages = tc.stages;
+    int32_t const ctas = tc.ctas;
+    // candidate cost models: the default first
+    std::vector<bfg::TcCostModel> models = {
+        {60, 1, 29}, {40, 1, 29}, {90, 1, 29}, {60, 3, 29}, {60, 0, 29}, {60, 1, 60}, {0, 0, 100}};
+    size_t const K = models.size();
+    std::vector<bfg::TcSchedule> cands(K);
+    for (size_t k = 0; k < K; ++k) {
+      bfg::makeTcSchedule(p128, terms, ctas, cands[k], models[k]);
+      if (cands[k].arenaBytes != cands[0].arenaBytes)
+        throw BfgError{BFG_ERROR_RUNTIME, "autotune: schedules disagree on the tiles"};
+    }
+    // scratch operands: the times do not depend on the values
+    bfg::ApplyProgram const &p = f->prog;
+    DevBuf xs;
+    ck(xs.ensure((size_t)std::max<int64_t>(1, p.numCols) * R * sizeof(float2)), "autotune");
+    ck(cudaMemsetAsync(xs.p, 0, (size_t)p.numCols * R * sizeof(float2), s), "autotune");
+    ck(f->ws.ensure((size_t)std::max<int64_t>(1, p.wsRows) * R * sizeof(float2)), "workspace");
+    std::vector<cudaEvent_t> ev(nStages + 1);
+    for (auto &e : ev) ck(cudaEventCreate(&e), "autotune");
+    int const reps = 5;
+    std::vector<std::vector<float>> best(K, std::vector<float>(nStages, 1e30f));
+    DevBuf dch, dc0;
+    for (size_t k = 0; k < K; ++k) {
+      upload(dch, cands[k].chunks, s, "autotune");
+      upload(dc0, cands[k].ctaChunk0, s, "autotune");
+      for (int rep = 0; rep < reps + 1; ++rep) {
+        ck(cudaEventRecord(ev[0], s), "autotune");
+        for (size_t st = 0; st < nStages; ++st) {
+          ck(bfg::launchApplyTc(terms, dch.as<bfg::TcChunk>(),
+                                dc0.as<int64_t>() + st * (size_t)(ctas + 1), ctas,
+                                tc.arena.as<uint8_t>(), xs.as<float2>(), R, f->ws.as<float2>(), R,
+                                f->tcStatus.as<int32_t>(), s),
+             "autotune");
+          ck(cudaEventRecord(ev[st + 1], s), "autotune");
+        }
+        ck(cudaStreamSynchronize(s), "autotune");
+        if (rep == 0) continue;   // warm-up
+        for (size_t st = 0; st < nStages; ++st) {
+          float ms = 0;
+          ck(cudaEventElapsedTime(&ms, ev[st], ev[st + 1]), "autotune");
+          best[k][st] = std::min(best[k][st], ms);
+        }
+      }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    checkTcStatus(f);
+    // per stage the fastest candidate, spliced into one schedule
+    std::vector<bfg::TcChunk> chunks;
+    std::vector<int64_t> c0;
+    for (size_t st = 0; st < nStages; ++st) {
+      size_t kb = 0;
+      for (size_t k = 1; k < K; ++k)
+        if (best[k][st] < best[kb][st]) kb = k;
+      bfg::TcSchedule const &c = cands[kb];
+      int64_t const a = c.ctaChunk0[st * (size_t)(ctas + 1)];
+      int64_t const b = c.ctaChunk0[st * (size_t)(ctas + 1) + ctas];
+      int64_t const base = (int64_t)chunks.size();
+      for (int32_t q = 0; q <= ctas; ++q) c0.push_back(c.ctaChunk0[st * (size_t)(ctas + 1) + q] - a + base);
+      chunks.insert(chunks.end(), c.chunks.begin() + a, c.chunks.begin() + b);
+      if (numStages) *numStages = (int32_t)nStages;
+      if ((int64_t)(2 * st + 1) < capacity) {
+        stageMs[2 * st] = best[0][st];
+        stageMs[2 * st + 1] = best[kb][st];
+      }
+    }
+    if (numStages) *numStages = (int32_t)nStages;
+    upload(tc.chunks, chunks, s, "tensor-core schedule");
+    upload(tc.ctaChunk0, c0, s, "tensor-core schedule");
+    ck(cudaStreamSynchronize(s), "tensor-core schedule");
+    return BFG_OK;
+  });
+}
+
 bfgStatus bfgFacPrepare(bfgFac f, bfgPrecision prec) {
   if (!f) return BFG_ERROR_INVALID_ARGUMENTS;
   if (prec < BFG_PRECISION_FP64 || prec > BFG_PRECISION_DF64)

@@ -888,7 +888,8 @@ void makeApplyProgram(Plan const &plan, ApplyProgram &prog, int itemRows) {
   }
 }
 
-void makeTcSchedule(ApplyProgram const &prog, int terms, int ctas, TcSchedule &sc) {
+void makeTcSchedule(ApplyProgram const &prog, int terms, int ctas, TcSchedule &sc,
+                    TcCostModel const &model) {
   sc = TcSchedule();
   sc.ctas = ctas;
   size_t const nStages = prog.stageItem0.empty() ? 0 : prog.stageItem0.size() - 1;
@@ -933,7 +934,8 @@ void makeTcSchedule(ApplyProgram const &prog, int terms, int ctas, TcSchedule &s
           // not the bytes)
           int64_t const ksteps = (k.kg + 1) / 2;
           cost[(size_t)(i - a)] += std::max<int64_t>(
-              60 + terms * ksteps, (int64_t)k.kg * mg * terms * 29 / 100);
+              model.perChunk + model.perKstep * terms * ksteps,
+              (int64_t)k.kg * mg * terms * model.bytesPct / 100);
         }
       }
       // every block has at least one column, so every item has a chunk

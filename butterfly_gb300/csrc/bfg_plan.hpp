@@ -241,10 +241,22 @@ struct TcSchedule {
   int32_t maxChunksPerCta = 0;
 };
 
+// Cost of a chunk for the longest-first dealing, in units of ~10 ns:
+// max(perChunk + perKstep * terms * ksteps, bytesPct / 100 * kg * mg * terms).
+// The defaults follow per-CTA durations measured on the GB300; the autotuner
+// (bfgFacAutotune) times other settings per stage.
+struct TcCostModel {
+  int64_t perChunk = 60;
+  int64_t perKstep = 1;
+  int64_t bytesPct = 29;
+};
+
 // Splits the 128-row program's items into chunks and deals each stage's items
 // to `ctas` CTAs, longest first to the least-loaded CTA.  Tile offsets are in
-// bytes for `terms` planes per tile.
-void makeTcSchedule(ApplyProgram const &prog128, int terms, int ctas, TcSchedule &sched);
+// bytes for `terms` planes per tile; they follow the item order, so every cost
+// model gives the same tiles.
+void makeTcSchedule(ApplyProgram const &prog128, int terms, int ctas, TcSchedule &sched,
+                    TcCostModel const &model = TcCostModel());
 
 // Fill descriptors for the kernel-evaluation and re-expansion kernels.
 struct FillDesc {

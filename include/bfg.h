@@ -183,6 +183,15 @@ bfgStatus bfgFacCopyBlocks(bfgFac fac, double *entries, int64_t capacityEntries,
 /* Builds the precision's copy of the factors now, as the first apply in that
  * precision would (allocates and synchronises). */
 bfgStatus bfgFacPrepare(bfgFac fac, bfgPrecision precision);
+/* Autotuner of the tensor-core apply (BF16X2, BF16X3): deals each stage's
+ * chunks to the persistent CTAs under several cost models, times every
+ * stage of every candidate on the GPU (numRhs right-hand sides, best of 5)
+ * and keeps, per stage, the fastest (the default model is a candidate, so
+ * no stage gets slower).  stageMs[2 s], stageMs[2 s + 1]: stage s with the
+ * default and the chosen schedule (up to `capacity` values); *numStages the
+ * number of stages.  Results do not change, only which CTA runs which chunk. */
+bfgStatus bfgFacAutotune(bfgFac fac, bfgPrecision precision, int64_t numRhs, double *stageMs,
+                         int32_t capacity, int32_t *numStages);
 
 /* Y = A X -- bfMatMul (mat.c:183-185) with A the factorization.  X (numCols
  * x numRhs) and Y (numRows x numRhs) are DEVICE pointers: complex128 for

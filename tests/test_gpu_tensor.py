@@ -155,3 +155,18 @@ def test_pipelined_host_apply_matches_synchronous(ctx, prec):
     ctx.check(lib.bfgFacApplyHostWait(fac.handle))
     for x, y in zip(Xs, Yp):
         assert np.array_equal(y.numpy(), fac.apply(x, precision=prec))
+
+
+def test_autotune_keeps_results_and_never_slows_a_stage(ctx):
+    """bfgFacAutotune re-deals chunks to CTAs; an item stays on one CTA with
+    its chunks in order, so the results are bit-identical."""
+    g, fac = golden_fac("ellipse_n16384_k128", ctx)
+    X = torch.from_numpy(O.RefRng(50).complex_randn(16384 * 16).reshape(16384, 16)).cuda()
+    X = X.to(torch.complex64)
+    y0 = fac.apply(X, precision="bf16x3")
+    times = fac.autotune("bf16x3", 16)
+    assert times.shape[0] == len(fac.launch_info()) - 1          # stages, not the final sum
+    assert np.all(times[:, 1] <= times[:, 0])
+    assert torch.equal(fac.apply(X, precision="bf16x3"), y0)
+    with pytest.raises(B.BfgError):
+        fac.autotune("fp32", 16)
