@@ -48,7 +48,8 @@ class _Helm2C(ctypes.Structure):
 class _FacOptionsC(ctypes.Structure):
     _fields_ = [("leafSize", ctypes.c_int64), ("rankEps", ctypes.c_double),
                 ("pinvCut", ctypes.c_int32), ("treeOnGpu", ctypes.c_int32),
-                ("pinvTol", ctypes.c_double)]
+                ("pinvTol", ctypes.c_double), ("jacobiArith", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 class _QuadtreeNodeC(ctypes.Structure):
@@ -282,7 +283,7 @@ class FacHelm2:
     @staticmethod
     def make_multilevel(helm: Helm2, src_tree: Quadtree, tgt_tree: Quadtree | None = None,
                         *, rank_eps: float = 1e-15, pinv_tol: float | None = None,
-                        tree_on_gpu: bool = False,
+                        tree_on_gpu: bool = False, jacobi: str = "fp64",
                         context: Context | None = None) -> "Fac":
         tgt_tree = src_tree if tgt_tree is None else tgt_tree
         if src_tree.leaf_size != tgt_tree.leaf_size:
@@ -295,6 +296,7 @@ class FacHelm2:
         opts.leafSize = int(src_tree.leaf_size)
         opts.rankEps = float(rank_eps)
         opts.treeOnGpu = 1 if tree_on_gpu else 0
+        opts.jacobiArith = {"fp64": 0, "df64": 1}[jacobi]
         if pinv_tol is not None:
             opts.pinvCut, opts.pinvTol = 1, float(pinv_tol)
         h = _VP()
@@ -307,7 +309,7 @@ class FacHelm2:
 
 def make_batched(helm: Helm2, problems, ks, *, leaf_size: int = 1, rank_eps: float = 1e-15,
                  pinv_tol: float | None = None, context: Context | None = None,
-                 tree_on_gpu: bool = False) -> "Fac":
+                 tree_on_gpu: bool = False, jacobi: str = "fp64") -> "Fac":
     """Factorize many independent problems in one go (bfgFacHelm2MakeBatched).
     ``problems``: list of (src, tgt) or (src, tgt, src_normals, tgt_normals);
     ``ks``: wavenumber per problem.  The result applies diag(A_0, ..., A_P-1);
@@ -331,6 +333,7 @@ def make_batched(helm: Helm2, problems, ks, *, leaf_size: int = 1, rank_eps: flo
     opts.leafSize = int(leaf_size)
     opts.rankEps = float(rank_eps)
     opts.treeOnGpu = 1 if tree_on_gpu else 0
+    opts.jacobiArith = {"fp64": 0, "df64": 1}[jacobi]
     if pinv_tol is not None:
         opts.pinvCut, opts.pinvTol = 1, float(pinv_tol)
     h = _VP()

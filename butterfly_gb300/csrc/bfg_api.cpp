@@ -314,12 +314,12 @@ void factorize(bfgFac f) {
   upload(dSmem8, reSmem8, s, "descriptors");
   ck(bfg::launchReexpansion(dSmem8.as<bfg::FillDesc>(), (int32_t)reSmem8.size(), src, kpProxy,
                             f->opts.pinvCut, f->opts.pinvTol, arena, nullptr, nullptr, nullptr,
-                            st, 0, maxBytes(reSmem8, 8, false), 256, s),
+                            st, 0, maxBytes(reSmem8, 8, false), 256, f->opts.jacobiArith, s),
      "re-expansion kernel");
   upload(dSmem16, reSmem16, s, "descriptors");
   ck(bfg::launchReexpansion(dSmem16.as<bfg::FillDesc>(), (int32_t)reSmem16.size(), src, kpProxy,
                             f->opts.pinvCut, f->opts.pinvTol, arena, nullptr, nullptr, nullptr,
-                            st, 0, maxBytes(reSmem16, 16, false), 512, s),
+                            st, 0, maxBytes(reSmem16, 16, false), 512, f->opts.jacobiArith, s),
      "re-expansion kernel");
   ck(cudaEventRecord(eSmem, s), "event");
 
@@ -348,7 +348,7 @@ void factorize(bfgFac f) {
       ck(bfg::launchReexpansion(dBatch.as<bfg::FillDesc>(), (int32_t)batch.size(), src, kpProxy,
                                 f->opts.pinvCut, f->opts.pinvTol, arena, scratch.as<double2>(),
                                 dScratchOff.as<int64_t>(), dFlags.as<int32_t>(), st, mode,
-                                maxBytes(batch, 0, true), 512, s),
+                                maxBytes(batch, 0, true), 512, f->opts.jacobiArith, s),
          mode == 1 ? "re-expansion kernel (global)" : "re-expansion kernel (cluster)");
       // the batch's descriptors, offsets and scratch are reused by the next
       ck(cudaStreamSynchronize(s), "re-expansion");
@@ -713,7 +713,7 @@ namespace {
 // arena (arenaEntries complex128 values in plan order).  All little-endian,
 // written as laid out in memory (the same layout on x86-64 and aarch64).
 constexpr char kFacMagic[8] = {'B', 'F', 'G', 'F', 'A', 'C', '\0', '\1'};
-constexpr uint32_t kFacVersion = 1;
+constexpr uint32_t kFacVersion = 2;   // 2: bfgFacOptions with jacobiArith
 
 struct FacFileHeader {
   char magic[8];
@@ -724,7 +724,7 @@ struct FacFileHeader {
   int32_t batched, srcHasNormals, tgtHasNormals, reserved2;
   int64_t nSrc, nTgt, arenaEntries;
 };
-static_assert(sizeof(FacFileHeader) == 144, "file header layout");
+static_assert(sizeof(FacFileHeader) == 152, "file header layout");
 
 constexpr int64_t kFileChunkEntries = int64_t(1) << 24;   // 256 MB of complex128
 
@@ -820,7 +820,8 @@ bfgStatus bfgFacHelm2MakeMultilevel(bfgContext ctx, bfgHelm2 const *helm, double
     bfgFacOptions o;
     bfgFacOptionsDefault(&o);
     if (opts) o = *opts;
-    if (o.leafSize < 1 || !(o.rankEps > 0 && o.rankEps < 1) || (o.pinvCut != 0 && o.pinvCut != 1) ||
+    if (o.leafSize < 1 || !(o.rankEps > 0 && o.rankEps < 1) || (o.pinvCut != 0 && o.pinvCut != 1) || (o.jacobiArith != 0 && o.jacobiArith != 1) ||
+        (o.jacobiArith == 1 && !(o.pinvCut == 1 && o.pinvTol >= 1e-12)) ||
         (o.pinvCut == 1 && !(o.pinvTol > 0 && o.pinvTol < 1)))
       return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "make: bad options");
     for (int64_t i = 0; i < 2 * numSrc; ++i)
@@ -901,7 +902,8 @@ bfgStatus bfgFacHelm2MakeBatched(bfgContext ctx, bfgHelm2 const *helm, double co
     bfgFacOptions o;
     bfgFacOptionsDefault(&o);
     if (opts) o = *opts;
-    if (o.leafSize < 1 || !(o.rankEps > 0 && o.rankEps < 1) || (o.pinvCut != 0 && o.pinvCut != 1) ||
+    if (o.leafSize < 1 || !(o.rankEps > 0 && o.rankEps < 1) || (o.pinvCut != 0 && o.pinvCut != 1) || (o.jacobiArith != 0 && o.jacobiArith != 1) ||
+        (o.jacobiArith == 1 && !(o.pinvCut == 1 && o.pinvTol >= 1e-12)) ||
         (o.pinvCut == 1 && !(o.pinvTol > 0 && o.pinvTol < 1)))
       return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "batched make: bad options");
     auto *f = new bfgFac_s;

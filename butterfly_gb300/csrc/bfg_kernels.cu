@@ -143,7 +143,49 @@ __global__ void fillBlocksKernel(FillDesc const *__restrict__ descs, PointsDev s
 // ---------------------------------------------------------------------------
 constexpr int kClusterCtas = 8;
 
-template <int kMode>
+// ---- double-float arithmetic for the Jacobi sweeps (kDf): each complex
+// entry of M held as FP32 pairs (re hi, re lo, im hi, im lo) in the same 16
+// bytes, products by FMA error terms, sums by TwoSum (Dekker; Knuth TAOCP
+// 4.2.2).  The _rn intrinsics are never contracted into FMAs, which would
+// break the error-free steps.
+__device__ __forceinline__ void jTwoSum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  float const bp = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+}
+// (sh, sl) += (ah + al)(bh + bl), unnormalised
+__device__ __forceinline__ void jMac(float ah, float al, float bh, float bl, float &sh, float &sl) {
+  float const ph = __fmul_rn(ah, bh);
+  float pl = fmaf(ah, bh, -ph);
+  pl = fmaf(ah, bl, pl);
+  pl = fmaf(al, bh, pl);
+  float s, e;
+  jTwoSum(sh, ph, s, e);
+  sh = s;
+  sl += e + pl;
+}
+__device__ __forceinline__ float2 jNorm(float h, float l) {
+  float const s = __fadd_rn(h, l);
+  return make_float2(s, __fsub_rn(l, __fsub_rn(s, h)));
+}
+__device__ __forceinline__ float2 jSplit(double d) {
+  float const h = __double2float_rn(d);
+  return make_float2(h, __double2float_rn(d - (double)h));
+}
+// the sum over the warp as a double; TwoSum is commutative, so every lane of
+// the butterfly gets the same bits
+__device__ __forceinline__ double jWarpSum(float h, float l) {
+  for (int o = 16; o > 0; o >>= 1) {
+    float const oh = __shfl_xor_sync(0xffffffffu, h, o), ol = __shfl_xor_sync(0xffffffffu, l, o);
+    float s, e;
+    jTwoSum(h, oh, s, e);
+    h = s;
+    l = __fadd_rn(e, __fadd_rn(l, ol));
+  }
+  return (double)h + (double)l;
+}
+
+template <int kMode, bool kDf>
 struct ReexpMem {
   static __device__ __forceinline__ double2 ld(double2 const *p) {
     if (kMode == 2) return __ldcg(p);   // other SMs of the cluster write M
@@ -153,18 +195,45 @@ struct ReexpMem {
     if (kMode == 2) __stcg(p, v);
     else *p = v;
   }
+  static __device__ __forceinline__ float4 ld4(double2 const *p) {
+    float4 const *q = reinterpret_cast<float4 const *>(p);
+    if (kMode == 2) return __ldcg(q);
+    return *q;
+  }
+  static __device__ __forceinline__ void st4(double2 *p, float4 v) {
+    float4 *q = reinterpret_cast<float4 *>(p);
+    if (kMode == 2) __stcg(q, v);
+    else *q = v;
+  }
+  // an entry of M as a complex double, whichever way it is held
+  static __device__ __forceinline__ double2 ldC(double2 const *p) {
+    if (!kDf) return ld(p);
+    float4 const v = ld4(p);
+    return make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+  }
+  static __device__ __forceinline__ void stC(double2 *p, double2 v) {
+    if (!kDf) {
+      st(p, v);
+      return;
+    }
+    float2 const r = jSplit(v.x), i = jSplit(v.y);
+    st4(p, make_float4(r.x, r.y, i.x, i.y));
+  }
   static __device__ __forceinline__ void sync() {
     if (kMode == 2) cooperative_groups::this_cluster().sync();
     else __syncthreads();
   }
 };
 
-template <int kMode>
+// kDf: the Jacobi sweeps in double-float (~48 significant bits, FP32
+// arithmetic, about 6x fewer FP64 instructions; the rotation angles, the
+// singular values and the output stay FP64), else in FP64
+template <int kMode, bool kDf>
 __global__ void __launch_bounds__(512) reexpansionKernel(
     FillDesc const *__restrict__ descs, PointsDev src, KernelParams kp, int32_t cutMode,
     double cutTol, double2 *arena, double2 *scratch, int64_t const *scratchOff,
     int32_t *flags, int32_t *status) {
-  using Mem = ReexpMem<kMode>;
+  using Mem = ReexpMem<kMode, kDf>;
   extern __shared__ double2 smem2[];
   int const ctas = kMode == 2 ? kClusterCtas : 1;
   int const blk = kMode == 2 ? (int)(blockIdx.x / kClusterCtas) : (int)blockIdx.x;
@@ -246,7 +315,7 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
       } else {
         v = make_double2(r - p == a ? 1.0 : 0.0, 0.0);
       }
-      Mem::st(M + e, v);
+      Mem::stC(M + e, v);
     }
   }
   Mem::sync();
@@ -254,7 +323,10 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
   // one-sided Jacobi, round-robin pair schedule
   int const P = p + (p & 1);
   int const nPairs = P / 2;
-  double const tolRot = kEps * sqrt((double)p);
+  // rotation threshold: FP64 eps, or (double-float) 2^-44, well above the
+  // rounding noise of the pair sums (2^-46 left a large block cycling to the
+  // sweep cap)
+  double const tolRot = (kDf ? 5.684341886080802e-14 : kEps) * sqrt((double)p);
   bool converged = false;
   for (int sweep = 0; sweep < kMaxSweeps; ++sweep) {
     if (tid == 0) sRotated = 0;
@@ -272,28 +344,88 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
         if (i >= p || j >= p) continue;
         double2 *ci = M + (int64_t)i * LD, *cj = M + (int64_t)j * LD;
         double al = 0, be = 0, gr = 0, gi = 0;
-        for (int r = lane; r < p; r += 32) {
-          double2 x = Mem::ld(ci + r), y = Mem::ld(cj + r);
-          al += x.x * x.x + x.y * x.y;
-          be += y.x * y.x + y.y * y.y;
-          gr += x.x * y.x + x.y * y.y;     // conj(x) y
-          gi += x.x * y.y - x.y * y.x;
+        if (kDf) {
+          float alh = 0, all = 0, beh = 0, bel = 0, grh = 0, grl = 0, gih = 0, gil = 0;
+          for (int r = lane; r < p; r += 32) {
+            float4 const x = Mem::ld4(ci + r), y = Mem::ld4(cj + r);
+            jMac(x.x, x.y, x.x, x.y, alh, all);
+            jMac(x.z, x.w, x.z, x.w, alh, all);
+            jMac(y.x, y.y, y.x, y.y, beh, bel);
+            jMac(y.z, y.w, y.z, y.w, beh, bel);
+            jMac(x.x, x.y, y.x, y.y, grh, grl);      // conj(x) y
+            jMac(x.z, x.w, y.z, y.w, grh, grl);
+            jMac(x.x, x.y, y.z, y.w, gih, gil);
+            jMac(-x.z, -x.w, y.x, y.y, gih, gil);
+          }
+          al = jWarpSum(alh, all);
+          be = jWarpSum(beh, bel);
+          gr = jWarpSum(grh, grl);
+          gi = jWarpSum(gih, gil);
+        } else {
+          for (int r = lane; r < p; r += 32) {
+            double2 x = Mem::ld(ci + r), y = Mem::ld(cj + r);
+            al += x.x * x.x + x.y * x.y;
+            be += y.x * y.x + y.y * y.y;
+            gr += x.x * y.x + x.y * y.y;     // conj(x) y
+            gi += x.x * y.y - x.y * y.x;
+          }
+          al = warpSum(al);
+          be = warpSum(be);
+          gr = warpSum(gr);
+          gi = warpSum(gi);
         }
-        al = warpSum(al);
-        be = warpSum(be);
-        gr = warpSum(gr);
-        gi = warpSum(gi);
         double const ag = sqrt(gr * gr + gi * gi);
-        if (ag > tolRot * sqrt(al * be) && ag > 0.0) {
+        // double-float: a column below 1e-14 of its partner in norm (or near
+        // FP32 underflow, where its sums lose their precision) lies far
+        // under the pseudo-inverse cut; rotating it only cycles on rounding
+        bool const negligible =
+            kDf && (fmin(al, be) <= 1e-28 * fmax(al, be) || fmin(al, be) < 1e-34);
+        if (!negligible && ag > tolRot * sqrt(al * be) && ag > 0.0) {
           double const zeta = (be - al) / (2.0 * ag);
           double const t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
           double const c = 1.0 / sqrt(1.0 + t * t), s = c * t;
           double const er = gr / ag, ei = -gi / ag;   // exp(-i phi) = conj(gamma)/|gamma|
-          for (int r = lane; r < LD; r += 32) {
-            double2 x = Mem::ld(ci + r), y = Mem::ld(cj + r);
-            double const ytr = y.x * er - y.y * ei, yti = y.x * ei + y.y * er;
-            Mem::st(ci + r, make_double2(c * x.x - s * ytr, c * x.y - s * yti));
-            Mem::st(cj + r, make_double2(s * x.x + c * ytr, s * x.y + c * yti));
+          if (kDf) {
+            float2 const cD = jSplit(c), sD = jSplit(s), erD = jSplit(er), eiD = jSplit(ei);
+            for (int r = lane; r < LD; r += 32) {
+              float4 const x = Mem::ld4(ci + r), y = Mem::ld4(cj + r);
+              float h, l;
+              // yt = y exp(-i phi)
+              h = 0.f, l = 0.f;
+              jMac(y.x, y.y, erD.x, erD.y, h, l);
+              jMac(-y.z, -y.w, eiD.x, eiD.y, h, l);
+              float2 const ytr = jNorm(h, l);
+              h = 0.f, l = 0.f;
+              jMac(y.x, y.y, eiD.x, eiD.y, h, l);
+              jMac(y.z, y.w, erD.x, erD.y, h, l);
+              float2 const yti = jNorm(h, l);
+              // x' = c x - s yt, y' = s x + c yt
+              h = 0.f, l = 0.f;
+              jMac(cD.x, cD.y, x.x, x.y, h, l);
+              jMac(-sD.x, -sD.y, ytr.x, ytr.y, h, l);
+              float2 const xr = jNorm(h, l);
+              h = 0.f, l = 0.f;
+              jMac(cD.x, cD.y, x.z, x.w, h, l);
+              jMac(-sD.x, -sD.y, yti.x, yti.y, h, l);
+              float2 const xi = jNorm(h, l);
+              h = 0.f, l = 0.f;
+              jMac(sD.x, sD.y, x.x, x.y, h, l);
+              jMac(cD.x, cD.y, ytr.x, ytr.y, h, l);
+              float2 const yr = jNorm(h, l);
+              h = 0.f, l = 0.f;
+              jMac(sD.x, sD.y, x.z, x.w, h, l);
+              jMac(cD.x, cD.y, yti.x, yti.y, h, l);
+              float2 const yi = jNorm(h, l);
+              Mem::st4(ci + r, make_float4(xr.x, xr.y, xi.x, xi.y));
+              Mem::st4(cj + r, make_float4(yr.x, yr.y, yi.x, yi.y));
+            }
+          } else {
+            for (int r = lane; r < LD; r += 32) {
+              double2 x = Mem::ld(ci + r), y = Mem::ld(cj + r);
+              double const ytr = y.x * er - y.y * ei, yti = y.x * ei + y.y * er;
+              Mem::st(ci + r, make_double2(c * x.x - s * ytr, c * x.y - s * yti));
+              Mem::st(cj + r, make_double2(s * x.x + c * ytr, s * x.y + c * yti));
+            }
           }
           if (lane == 0) sRotated = 1;
         }
@@ -324,7 +456,7 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
     double2 const *ca = M + (int64_t)a * LD;
     double s2 = 0;
     for (int r = lane; r < p; r += 32) {
-      double2 v = Mem::ld(ca + r);
+      double2 v = Mem::ldC(ca + r);
       s2 += v.x * v.x + v.y * v.y;
     }
     s2 = warpSum(s2);
@@ -365,7 +497,7 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
       double2 const *qa = M + (int64_t)a * LD + p;
       double yr = 0, yi = 0;
       for (int r = lane; r < p; r += 32) {
-        double2 q = Mem::ld(qa + r), z = myB[r];
+        double2 q = Mem::ldC(qa + r), z = myB[r];
         yr += q.x * z.x + q.y * z.y;        // conj(q) z
         yi += q.x * z.y - q.y * z.x;
       }
@@ -379,7 +511,7 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
       for (int a = 0; a < p; ++a) {
         double2 const y = myY[a];
         if (y.x == 0.0 && y.y == 0.0) continue;
-        double2 const t = Mem::ld(M + (int64_t)a * LD + i);
+        double2 const t = Mem::ldC(M + (int64_t)a * LD + i);
         sr += t.x * y.x - t.y * y.y;
         si += t.x * y.y + t.y * y.x;
       }
@@ -874,27 +1006,28 @@ cudaError_t launchFillBlocks(FillDesc const *descs, int32_t nDesc, PointsDev src
   return cudaGetLastError();
 }
 
-cudaError_t launchReexpansion(FillDesc const *descs, int32_t nDesc, PointsDev src,
-                              KernelParams kp, int32_t cutMode, double cutTol,
-                              double2 *arena, double2 *scratch, int64_t const *scratchOff,
-                              int32_t *flags, int32_t *status, int32_t mode,
-                              int32_t smemBytes, int32_t threads, cudaStream_t stream) {
+template <bool kDf>
+cudaError_t launchReexpansionT(FillDesc const *descs, int32_t nDesc, PointsDev src,
+                               KernelParams kp, int32_t cutMode, double cutTol,
+                               double2 *arena, double2 *scratch, int64_t const *scratchOff,
+                               int32_t *flags, int32_t *status, int32_t mode,
+                               int32_t smemBytes, int32_t threads, cudaStream_t stream) {
   if (nDesc == 0) return cudaSuccess;
   cudaError_t e;
   if (mode == 0) {
-    e = cudaFuncSetAttribute(reexpansionKernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(reexpansionKernel<0, kDf>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              smemBytes);
     if (e != cudaSuccess) return e;
-    reexpansionKernel<0><<<nDesc, threads, smemBytes, stream>>>(
+    reexpansionKernel<0, kDf><<<nDesc, threads, smemBytes, stream>>>(
         descs, src, kp, cutMode, cutTol, arena, scratch, scratchOff, flags, status);
   } else if (mode == 1) {
-    e = cudaFuncSetAttribute(reexpansionKernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(reexpansionKernel<1, kDf>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              smemBytes);
     if (e != cudaSuccess) return e;
-    reexpansionKernel<1><<<nDesc, threads, smemBytes, stream>>>(
+    reexpansionKernel<1, kDf><<<nDesc, threads, smemBytes, stream>>>(
         descs, src, kp, cutMode, cutTol, arena, scratch, scratchOff, flags, status);
   } else {
-    e = cudaFuncSetAttribute(reexpansionKernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(reexpansionKernel<2, kDf>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              smemBytes);
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
@@ -909,11 +1042,24 @@ cudaError_t launchReexpansion(FillDesc const *descs, int32_t nDesc, PointsDev sr
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    e = cudaLaunchKernelEx(&cfg, reexpansionKernel<2>, descs, src, kp, cutMode, cutTol, arena,
-                           scratch, scratchOff, flags, status);
+    e = cudaLaunchKernelEx(&cfg, reexpansionKernel<2, kDf>, descs, src, kp, cutMode, cutTol,
+                           arena, scratch, scratchOff, flags, status);
     if (e != cudaSuccess) return e;
   }
   return cudaGetLastError();
+}
+
+cudaError_t launchReexpansion(FillDesc const *descs, int32_t nDesc, PointsDev src,
+                              KernelParams kp, int32_t cutMode, double cutTol,
+                              double2 *arena, double2 *scratch, int64_t const *scratchOff,
+                              int32_t *flags, int32_t *status, int32_t mode,
+                              int32_t smemBytes, int32_t threads, int32_t doubleFloat,
+                              cudaStream_t stream) {
+  if (doubleFloat)
+    return launchReexpansionT<true>(descs, nDesc, src, kp, cutMode, cutTol, arena, scratch,
+                                    scratchOff, flags, status, mode, smemBytes, threads, stream);
+  return launchReexpansionT<false>(descs, nDesc, src, kp, cutMode, cutTol, arena, scratch,
+                                   scratchOff, flags, status, mode, smemBytes, threads, stream);
 }
 
 cudaError_t launchDenseRows(PointsDev src, int64_t nSrc, PointsDev tgt,

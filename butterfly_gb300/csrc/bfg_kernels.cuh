@@ -52,7 +52,8 @@ cudaError_t launchReexpansion(FillDesc const *descs, int32_t nDesc, PointsDev sr
                               KernelParams kp, int32_t cutMode, double cutTol,
                               double2 *arena, double2 *scratch, int64_t const *scratchOff,
                               int32_t *flags, int32_t *status, int32_t mode,
-                              int32_t smemBytes, int32_t threads, cudaStream_t stream);
+                              int32_t smemBytes, int32_t threads, int32_t doubleFloat,
+                              cudaStream_t stream);
 
 int64_t reexpansionSmemBytes(int32_t m, int32_t n, int32_t warps);
 int64_t reexpansionGeoBytes(int32_t m, int32_t n);

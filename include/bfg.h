@@ -88,6 +88,13 @@ typedef struct bfgFacOptions {
   int32_t treeOnGpu;  /* 1: build the quadtrees on the GPU (the same trees
                          as the host build, which is the default, 0) */
   double pinvTol;
+  int32_t jacobiArith; /* arithmetic of the re-expansion SVDs' Jacobi sweeps:
+                          0 FP64 (default), 1 double-float (FP32 pairs,
+                          ~48 bits; several times faster on GB300, whose FP64
+                          units run at 1/64 of FP32).  Double-float resolves
+                          singular values to ~1e-14 of the largest, so it
+                          requires pinvCut = 1 with pinvTol >= 1e-12 */
+  int32_t reserved;
 } bfgFacOptions;
 
 typedef struct bfgFacStats {
