@@ -60,6 +60,37 @@ METRIC = "Butterfly apply RHS/s at 1e-6 rel err vs plain FP64 GPU; GMRES time-to
 NCU_DRAM_PER_ALG = {("fp32", 16, 5): [0.7973, 1.0266, 0.9855, 0.7925],
                     ("bf16x3", 16, 5): [0.8888, 1.0627, 1.0246, 1.0386]}
 ERR_BOUND = 1e-6
+# GB300's dense FP64 rate (nominal; no measured FP64 peak is available)
+FP64_NOMINAL_TFLOPS = 1.25
+
+
+def factorization_work(table, st):
+    """The factorization's unit counts and rates from its block table
+    (rows kind, m, n; kinds 0..3 = FIRST, MIDDLE, LAST, DENSE) and stats.
+
+    Kernel evaluations: m n per LAST/DENSE block (the fill kernel) and
+    p^2 + p n per FIRST/MIDDLE block of rank p (Z_equiv p x p and Z_orig
+    p x n, evaluated inside the re-expansion kernels; helm2.c:321-365).
+    SVD work: the model 22 p^3 flops for the SVD of Z_equiv plus 16 p^2 n for
+    applying its pseudo-inverse to Z_orig (two complex p x p products per
+    column); the Jacobi's executed flops grow with its sweep count, which the
+    model leaves out."""
+    kind = table[:, 0]
+    m = table[:, 1].astype(np.float64)
+    n = table[:, 2].astype(np.float64)
+    fm = kind <= 1
+    fill = float(np.sum(m[~fm] * n[~fm]))
+    proxy = float(np.sum(m[fm] * m[fm] + m[fm] * n[fm]))
+    svd = float(np.sum(22.0 * m[fm] ** 3 + 16.0 * m[fm] ** 2 * n[fm]))
+    reexp_s = (st["reexpSmemMs"] + st["reexpGlobalMs"]) / 1e3
+    tflops = svd / reexp_s / 1e12 if reexp_s > 0 else None
+    return {"kernel_evals": fill + proxy, "fill_evals": fill, "proxy_evals": proxy,
+            "fill_evals_per_s": fill / (st["fillMs"] / 1e3) if st["fillMs"] > 0 else None,
+            "svd_flops_model": svd,
+            "svd_model": "22 p^3 + 16 p^2 n per FIRST/MIDDLE block (rank p, n columns)",
+            "reexp_tflops_model": tflops, "fp64_peak_tflops": FP64_NOMINAL_TFLOPS,
+            "fp64_peak_source": "nominal",
+            "frac_of_nominal_fp64": tflops / FP64_NOMINAL_TFLOPS if tflops else None}
 
 
 def parse():
@@ -341,7 +372,8 @@ def run_batched(args, cfg):
             "err_bound": ERR_BOUND, "err_sample": "64 rows of each of %d problems" % len(ref),
             "factorization": {"wall_s": fac_s, "device_ms": st["factorMs"],
                               "blocks": st["numBlocks"], "bytes_fp64": fac.num_bytes(),
-                              "max_rank": st["maxRank"]},
+                              "max_rank": st["maxRank"],
+                              "work": factorization_work(fac.block_table(), st)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
                          "kernel": "apply launch %d of %d" % (dom, len(per)),
@@ -743,7 +775,8 @@ def main():
             "factorization": {"wall_s": fac_wall_s, "device_ms": st["factorMs"],
                               "blocks": st["numBlocks"], "bytes_fp64": fac.num_bytes(),
                               "max_rank": st["maxRank"],
-                              "jacobi_not_converged": st["jacobiNotConverged"]},
+                              "jacobi_not_converged": st["jacobiNotConverged"],
+                              "work": factorization_work(fac.block_table(), st)},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": launches, "gmres": gm, "autotune": tuned}
     print(json.dumps(line))

@@ -424,6 +424,13 @@ class Fac:
                                               _ptr(tab), st["numBlocks"]))
         return tab, ent
 
+    def block_table(self) -> np.ndarray:
+        """Rows (kind, m, n, offset) of every stored block in plan order,
+        without copying the factors; kinds 0..3 = FIRST, MIDDLE, LAST, DENSE."""
+        tab = np.empty((self.stats()["numBlocks"], 4), dtype=np.int64)
+        self.ctx.check(lib().bfgFacCopyBlocks(self.handle, None, 0, _ptr(tab), len(tab)))
+        return tab
+
     # -- apply -------------------------------------------------------------
     def save(self, path: str):
         """Writes the factorization (inputs and FP64 factors) to ``path``;

@@ -230,6 +230,10 @@ bfg::FillDesc toDesc(bfg::Block const &b) {
 }
 
 constexpr int64_t kSmemLimit = 220 * 1024;
+// smallest relative pseudo-inverse cut the double-float Jacobi accepts: its
+// columns carry rounding noise at ~1e-14 of the largest, and kept singular
+// vectors closer to it than 1e4x do not settle within the sweep cap
+constexpr double kDfJacobiMinCut = 1e-10;
 constexpr int64_t kScratchBudgetEntries = (int64_t)1 << 27;   // 2 GiB of complex128
 // ranks from which a block that misses shared memory gets a whole cluster
 constexpr int32_t kClusterMinRank = 128;
@@ -821,7 +825,7 @@ bfgStatus bfgFacHelm2MakeMultilevel(bfgContext ctx, bfgHelm2 const *helm, double
     bfgFacOptionsDefault(&o);
     if (opts) o = *opts;
     if (o.leafSize < 1 || !(o.rankEps > 0 && o.rankEps < 1) || (o.pinvCut != 0 && o.pinvCut != 1) || (o.jacobiArith != 0 && o.jacobiArith != 1) ||
-        (o.jacobiArith == 1 && !(o.pinvCut == 1 && o.pinvTol >= 1e-12)) ||
+        (o.jacobiArith == 1 && !(o.pinvCut == 1 && o.pinvTol >= kDfJacobiMinCut)) ||
         (o.pinvCut == 1 && !(o.pinvTol > 0 && o.pinvTol < 1)))
       return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "make: bad options");
     for (int64_t i = 0; i < 2 * numSrc; ++i)
@@ -903,7 +907,7 @@ bfgStatus bfgFacHelm2MakeBatched(bfgContext ctx, bfgHelm2 const *helm, double co
     bfgFacOptionsDefault(&o);
     if (opts) o = *opts;
     if (o.leafSize < 1 || !(o.rankEps > 0 && o.rankEps < 1) || (o.pinvCut != 0 && o.pinvCut != 1) || (o.jacobiArith != 0 && o.jacobiArith != 1) ||
-        (o.jacobiArith == 1 && !(o.pinvCut == 1 && o.pinvTol >= 1e-12)) ||
+        (o.jacobiArith == 1 && !(o.pinvCut == 1 && o.pinvTol >= kDfJacobiMinCut)) ||
         (o.pinvCut == 1 && !(o.pinvTol > 0 && o.pinvTol < 1)))
       return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "batched make: bad options");
     auto *f = new bfgFac_s;

@@ -225,6 +225,42 @@ struct ReexpMem {
   }
 };
 
+constexpr int kNoExp = -100000;   // no nonzero entry seen
+constexpr int kColExpBias = 1100;  // makes ilogb of any positive double positive
+
+// The double-float scale exponent s of a block: the largest e over its
+// threads (|entry|^2 < 2^e) and the largest s with p^2 2^(e + 2s) <= 2^100,
+// so that a column's squared norm stays below 2^100 / p (FP32 reaches 2^128)
+// while its rounding-floor entries stay far above 2^-102, where the error
+// terms of their products turn subnormal.  Mode 2 combines the cluster's
+// CTAs through their flag slots (free until the first sweep ends); every
+// thread of the block (or cluster) gets the same s.
+template <int kMode>
+__device__ int reexpScaleExp(int eTop, int p, int32_t *clusterFlags, int rank) {
+  __shared__ int red[32];
+  for (int o = 16; o > 0; o >>= 1) eTop = max(eTop, __shfl_xor_sync(0xffffffffu, eTop, o));
+  int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nWarps = blockDim.x >> 5;
+  if (lane == 0) red[warp] = eTop;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int m = kNoExp;
+    for (int w = 0; w < nWarps; ++w) m = max(m, red[w]);
+    red[0] = m;
+    if (kMode == 2) __stcg(clusterFlags + rank, m);
+  }
+  if (kMode == 2) cooperative_groups::this_cluster().sync();
+  else __syncthreads();
+  int eMax = red[0];
+  if (kMode == 2)
+    for (int q = 0; q < kClusterCtas; ++q) eMax = max(eMax, __ldcg(clusterFlags + q));
+  __syncthreads();   // red[] is read before any later use of the helper's storage
+  if (eMax == kNoExp) return 0;
+  int lp = 0;
+  while ((1 << lp) < p) ++lp;
+  int const t = 100 - 2 * lp - eMax;
+  return t >= 0 ? t / 2 : -((1 - t) / 2);
+}
+
 // kDf: the Jacobi sweeps in double-float (~48 significant bits, FP32
 // arithmetic, about 6x fewer FP64 instructions; the rotation angles, the
 // singular values and the output stay FP64), else in FP64
@@ -265,6 +301,7 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
   double *orX = geo + 6 * p, *orY = orX + n, *orNx = orX + 2 * n, *orNy = orX + 3 * n;
   double *wgt = orX + 4 * n;
   __shared__ int sRotated;
+  __shared__ unsigned long long sColMax;   // bits of a nonnegative double
   bool const useSrcN = kp.layerPot == kLpPvDouble || kp.layerPot == kLpCombinedField;
 
   // proxy geometry (every CTA of a cluster keeps its own copy); check points
@@ -303,19 +340,39 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
   }
   __syncthreads();
 
-  // M[a*LD + r] = conj(K(chk_a, eq_r)) for r < p, identity below
+  // M[a*LD + r] = conj(K(chk_a, eq_r)) for r < p, identity below.
+  // Double-float holds the top part scaled by 2^sExp (exact), sExp chosen
+  // from the largest entry so that the sweeps' products stay far above
+  // FP32's subnormal range: there the products' error terms lose their bits,
+  // and pairs of columns at the rounding floor (sigma^2 ~ 1e-31 of the
+  // largest) rotate on noise until the sweep cap.  FP64 keeps sExp = 0.
+  int sExp = 0;
   {
     int64_t const total = (int64_t)LD * p;
+    int eTop = kNoExp;   // exponent bound of the largest |entry|^2 this thread wrote
     for (int64_t e = (int64_t)rank * nthr + tid; e < total; e += (int64_t)ctas * nthr) {
       int const a = (int)(e / LD), r = (int)(e % LD);
       double2 v;
       if (r < p) {
         double2 k = kernelValue(kp, chkX[a], chkY[a], 0.0, 0.0, eqX[r], eqY[r], eqNx[r], eqNy[r]);
         v = make_double2(k.x, -k.y);
+        double const m2 = v.x * v.x + v.y * v.y;
+        if (kDf && m2 > 0.0) eTop = max(eTop, ilogb(m2) + 1);
       } else {
         v = make_double2(r - p == a ? 1.0 : 0.0, 0.0);
       }
-      Mem::stC(M + e, v);
+      if (kDf) Mem::st(M + e, v);   // FP64 until the scale is known
+      else Mem::stC(M + e, v);
+    }
+    if (kDf) {
+      sExp = reexpScaleExp<kMode>(eTop, p, flags ? flags + (int64_t)blk * kClusterCtas : nullptr,
+                                  rank);
+      // every thread converts the entries it wrote
+      for (int64_t e = (int64_t)rank * nthr + tid; e < total; e += (int64_t)ctas * nthr) {
+        double2 v = Mem::ld(M + e);
+        if ((int)(e % LD) < p) v = make_double2(ldexp(v.x, sExp), ldexp(v.y, sExp));
+        Mem::stC(M + e, v);
+      }
     }
   }
   Mem::sync();
@@ -327,10 +384,27 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
   // rounding noise of the pair sums (2^-46 left a large block cycling to the
   // sweep cap)
   double const tolRot = (kDf ? 5.684341886080802e-14 : kEps) * sqrt((double)p);
+  // double-float: columns far under the pseudo-inverse cut carry the
+  // rounding noise (2^-48 of the largest columns) that every rotation of a
+  // large column injects, and rotations on that noise would go on to the
+  // sweep cap.  Measured against the previous sweep's largest column norm^2
+  // (a lower bound of sigma_max^2): a pair whose columns both lie below
+  // 1e-4 cut^2 is not rotated (only rotations with larger columns, which
+  // still run, could lift them toward the cut), and one whose columns both
+  // lie below 1e-2 cut^2 is rotated without holding the sweeps open --
+  // neither can change the kept part of the pseudo-inverse.
+  // The second band keeps a column just above the first from cycling against
+  // the unrotated noise columns until the cap.
+  double const cutRel = cutMode == 0 ? (double)p * kEps : cutTol;
+  double skipBelow = 0.0, quietBelow = 0.0;
   bool converged = false;
   for (int sweep = 0; sweep < kMaxSweeps; ++sweep) {
-    if (tid == 0) sRotated = 0;
+    if (tid == 0) {
+      sRotated = 0;
+      sColMax = 0ull;
+    }
     __syncthreads();
+    double colMax = 0.0;   // this warp's largest column norm^2 of the sweep
     for (int round = 0; round < P - 1; ++round) {
       for (int pr = gWarp; pr < nPairs; pr += gWarps) {
         int i, j;
@@ -375,11 +449,11 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
           gi = warpSum(gi);
         }
         double const ag = sqrt(gr * gr + gi * gi);
-        // double-float: a column below 1e-14 of its partner in norm (or near
-        // FP32 underflow, where its sums lose their precision) lies far
+        // double-float: a column below 1e-14 of its partner in norm lies far
         // under the pseudo-inverse cut; rotating it only cycles on rounding
+        if (kDf) colMax = fmax(colMax, fmax(al, be));
         bool const negligible =
-            kDf && (fmin(al, be) <= 1e-28 * fmax(al, be) || fmin(al, be) < 1e-34);
+            kDf && (fmin(al, be) <= 1e-28 * fmax(al, be) || fmax(al, be) < skipBelow);
         if (!negligible && ag > tolRot * sqrt(al * be) && ag > 0.0) {
           double const zeta = (be - al) / (2.0 * ag);
           double const t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
@@ -427,25 +501,44 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
               Mem::st(cj + r, make_double2(s * x.x + c * ytr, s * x.y + c * yti));
             }
           }
-          if (lane == 0) sRotated = 1;
+          if (lane == 0 && (!kDf || fmax(al, be) >= quietBelow)) sRotated = 1;
         }
       }
       Mem::sync();
     }
+    if (kDf) {
+      if (lane == 0) atomicMax(&sColMax, (unsigned long long)__double_as_longlong(colMax));
+      __syncthreads();
+    }
     int rotated = sRotated;
+    // the largest column norm^2 as a biased exponent (2^(colExp - bias) <= it)
+    int colExp = 0;
+    if (kDf) {
+      double const cm = __longlong_as_double((long long)sColMax);
+      colExp = cm > 0.0 ? ilogb(cm) + kColExpBias : 0;
+    }
     if (kMode == 2) {
-      // cluster-wide OR of the CTAs' flags, read after a barrier so every CTA
-      // takes the same exit decision
-      if (tid == 0) __stcg(flags + (int64_t)blk * kClusterCtas + rank, rotated);
+      // cluster-wide OR of the CTAs' flags (and maximum of their exponents),
+      // read after a barrier so every CTA takes the same decisions
+      if (tid == 0) __stcg(flags + (int64_t)blk * kClusterCtas + rank, rotated | (colExp << 1));
       Mem::sync();
       rotated = 0;
-      for (int q = 0; q < kClusterCtas; ++q)
-        rotated |= __ldcg(flags + (int64_t)blk * kClusterCtas + q);
+      colExp = 0;
+      for (int q = 0; q < kClusterCtas; ++q) {
+        int const v = __ldcg(flags + (int64_t)blk * kClusterCtas + q);
+        rotated |= v & 1;
+        colExp = max(colExp, v >> 1);
+      }
     }
     __syncthreads();
     if (!rotated) {
       converged = true;
       break;
+    }
+    if (kDf && colExp > 0) {
+      double const colMaxLow = ldexp(cutRel * cutRel, colExp - kColExpBias);
+      skipBelow = 1e-4 * colMaxLow;
+      quietBelow = 1e-2 * colMaxLow;
     }
   }
   if (!converged && tid == 0 && rank == 0) atomicOr(status, kStatusJacobiNotConverged);
@@ -460,6 +553,7 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
       s2 += v.x * v.x + v.y * v.y;
     }
     s2 = warpSum(s2);
+    if (kDf) s2 = ldexp(s2, -2 * sExp);   // sigma^2 of the unscaled block
     if (lane == 0) {
       if (kMode == 2) Mem::st(wg + a, make_double2(s2, 0.0));
       else wgt[a] = s2;
@@ -475,7 +569,8 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
     double const cut = cutMode == 0 ? (double)p * kEps * smax + kEps : cutTol * smax;
     for (int a = 0; a < p; ++a) {
       double const sa = sqrt(wgt[a]);
-      wgt[a] = (sa < cut || sa == 0.0) ? 0.0 : 1.0 / wgt[a];
+      // (double-float: T holds 2^sExp of its columns, so 2^-sExp goes here)
+      wgt[a] = (sa < cut || sa == 0.0) ? 0.0 : ldexp(1.0 / wgt[a], -sExp);
     }
   }
   __syncthreads();

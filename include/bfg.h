@@ -91,9 +91,10 @@ typedef struct bfgFacOptions {
   int32_t jacobiArith; /* arithmetic of the re-expansion SVDs' Jacobi sweeps:
                           0 FP64 (default), 1 double-float (FP32 pairs,
                           ~48 bits; several times faster on GB300, whose FP64
-                          units run at 1/64 of FP32).  Double-float resolves
-                          singular values to ~1e-14 of the largest, so it
-                          requires pinvCut = 1 with pinvTol >= 1e-12 */
+                          units run at 1/64 of FP32).  Double-float carries
+                          rounding noise at ~1e-14 of the largest singular
+                          value, so it requires pinvCut = 1 with
+                          pinvTol >= 1e-10 */
   int32_t reserved;
 } bfgFacOptions;
 
@@ -105,7 +106,7 @@ typedef struct bfgFacStats {
   int64_t numStages;          /* apply launches before the final sum */
   int64_t numItems;           /* apply work items over all stages */
   int64_t maxRank;
-  int64_t jacobiNotConverged; /* blocks whose Jacobi SVD hit the sweep cap */
+  int64_t jacobiNotConverged; /* 1 if any block's Jacobi SVD hit the sweep cap */
   double factorMs;            /* device time of the factorization kernels */
   double flopsPerRhs;         /* 8 * sum over blocks of m*n */
   double fillMs;              /* evaluation and dense blocks */

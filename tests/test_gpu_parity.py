@@ -157,6 +157,7 @@ def test_blocks_solve_the_reexpansion_least_squares(ctx):
     g, fac = golden_fac("star_n2048_k48", ctx)
     of = _oracle_fac("star_n2048_k48")
     tab, ent = fac.blocks()
+    assert np.array_equal(fac.block_table(), tab)   # the table-only query
     oblocks = of.blocks()
     assert len(oblocks) == len(tab)
     checked = 0

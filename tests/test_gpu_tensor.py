@@ -175,7 +175,7 @@ def test_autotune_keeps_results_and_never_slows_a_stage(ctx):
 def test_double_float_jacobi_factorization(ctx):
     """The re-expansion SVDs' Jacobi sweeps in double-float: the same
     operator as with FP64 sweeps (relative cut 1e-10), checked against dense
-    FP64 kernel rows; an eps-level cut is refused."""
+    FP64 kernel rows; every block converges; cuts below 1e-10 are refused."""
     src = O.uniform_square_points(6000, 4)
     tgt = O.curve_points("ellipse", 6000)
     X = torch.from_numpy(O.RefRng(60).complex_randn(6000 * 4).reshape(6000, 4)).cuda()
@@ -183,12 +183,19 @@ def test_double_float_jacobi_factorization(ctx):
                                           B.Quadtree(tgt, leaf_size=32), rank_eps=1e-10,
                                           pinv_tol=1e-10, jacobi=a, context=ctx)
             for a in ("fp64", "df64")}
+    # every block converges within the sweep cap in both arithmetics (this
+    # problem has blocks in every re-expansion mode, ranks up to 361)
+    assert facs["fp64"].stats()["jacobiNotConverged"] == 0
+    assert facs["df64"].stats()["jacobiNotConverged"] == 0
     y64 = facs["fp64"].apply(X).cpu().numpy()
     ydf = facs["df64"].apply(X).cpu().numpy()
     assert rel_err(ydf, y64) < 1e-9
     rows = np.arange(0, 6000, 97)
     yd = facs["df64"].dense_rows(rows, X, 4).cpu().numpy()
     assert rel_err(ydf[rows], yd) < 1e-8
-    with pytest.raises(B.BfgError):
-        B.FacHelm2.make_multilevel(B.Helm2(80.0), B.Quadtree(src, leaf_size=32),
-                                   B.Quadtree(tgt, leaf_size=32), jacobi="df64", context=ctx)
+    for tol in (None, 1e-11):   # the eps-level default cut, and one below 1e-10
+        kw = {} if tol is None else {"pinv_tol": tol}
+        with pytest.raises(B.BfgError):
+            B.FacHelm2.make_multilevel(B.Helm2(80.0), B.Quadtree(src, leaf_size=32),
+                                       B.Quadtree(tgt, leaf_size=32), jacobi="df64",
+                                       context=ctx, **kw)

@@ -102,3 +102,34 @@ def test_host_entry_points_reject_bad_input():
         B.plan_helm2(-1.0, np.zeros((4, 2)), np.ones((4, 2)))
     with pytest.raises(ValueError):
         B.plan_helm2(1.0, np.zeros((4, 3)), np.ones((4, 2)))
+
+
+# every struct the Python mirror passes across the C ABI, by its C name
+ABI_STRUCTS = [("bfgHelm2", "_Helm2C"), ("bfgFacOptions", "_FacOptionsC"),
+               ("bfgFacStats", "_FacStatsC"), ("bfgQuadtreeNode", "_QuadtreeNodeC"),
+               ("bfgGmresResult", "_GmresResultC"), ("bfgRng", "_RngC")]
+
+
+def test_ctypes_structs_match_header(tmp_path):
+    """The ctypes mirrors have the header's size and every field at the
+    header's offset with the header's size (a C program compiled against
+    include/bfg.h prints them)."""
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "bfg.h"', 'int main(void) {']
+    want = []
+    for cname, pyname in ABI_STRUCTS:
+        cls = getattr(B, pyname)
+        lines.append('  printf("%%s %%zu\\n", "%s", sizeof(%s));' % (cname, cname))
+        want.append("%s %d" % (cname, ctypes.sizeof(cls)))
+        for fname, _ in cls._fields_:
+            lines.append('  printf("%%s.%%s %%zu %%zu\\n", "%s", "%s", offsetof(%s, %s), '
+                         'sizeof(((%s *)0)->%s));' % (cname, fname, cname, fname, cname, fname))
+            f = getattr(cls, fname)
+            want.append("%s.%s %d %d" % (cname, fname, f.offset, f.size))
+    lines += ['  return 0;', '}']
+    src = tmp_path / "abi.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "abi"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                    str(exe)], check=True)
+    got = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    assert [g for g in got if g] == want
