@@ -1,0 +1,77 @@
+"""CPU tests of the bench's host-side parts: the factorization work counts
+(kernel evaluations, the SVD flop model) on a hand-made block table, and the
+reference arm's JSON line (the oracle's C port of the reference's apply on
+host cores), which needs no GPU."""
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+import bench
+from conftest import ROOT
+
+
+def test_factorization_work_counts_and_rates():
+    # FIRST 4 x 10, MIDDLE 3 x 8, LAST 5 x 3, DENSE 2 x 2
+    table = np.array([[0, 4, 10, 0], [1, 3, 8, 40], [2, 5, 3, 64], [3, 2, 2, 79]], np.int64)
+    st = {"fillMs": 2.0, "reexpSmemMs": 1.0, "reexpGlobalMs": 3.0}
+    w = bench.factorization_work(table, st)
+    assert w["fill_evals"] == 5 * 3 + 2 * 2
+    assert w["proxy_evals"] == (16 + 40) + (9 + 24)
+    assert w["kernel_evals"] == w["fill_evals"] + w["proxy_evals"]
+    assert w["fill_evals_per_s"] == 19 / 2e-3
+    svd = 22 * 4 ** 3 + 16 * 16 * 10 + 22 * 3 ** 3 + 16 * 9 * 8
+    assert w["svd_flops_model"] == svd
+    assert np.isclose(w["reexp_tflops_model"], svd / 4e-3 / 1e12)
+    assert np.isclose(w["frac_of_nominal_fp64"], w["reexp_tflops_model"] / 1.25)
+
+
+def test_factorization_work_without_reexpansions():
+    table = np.array([[3, 6, 6, 0]], np.int64)
+    w = bench.factorization_work(table, {"fillMs": 1.0, "reexpSmemMs": 0.0, "reexpGlobalMs": 0.0})
+    assert w["kernel_evals"] == 36 and w["svd_flops_model"] == 0
+    assert w["reexp_tflops_model"] is None and w["frac_of_nominal_fp64"] is None
+
+
+def _bench(args, **env):
+    e = dict(os.environ)
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
+        e.pop(k, None)
+    e.update(env)
+    return subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), *args], cwd=ROOT,
+                          env=e, capture_output=True, text=True, timeout=300)
+
+
+def test_reference_arm_prints_the_contract_line():
+    r = _bench(["--impl", "reference", "--config", "c1", "--steps", "2", "--warmup", "3"])
+    assert r.returncode == 0, r.stderr
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference" and line["metric"] == bench.METRIC
+    assert line["unit"] == "RHS/s" and line["higher_is_better"] is True
+    assert line["value"] > 0 and line["ms_per_step"] > 0
+    assert (line["n_gpus"], line["steps"], line["warmup"]) == (1, 2, 3)
+    assert line["scaling"] == "weak" and line["vs_baseline"] is None
+    assert line["config"]["workload"] == "helmholtz2d_butterfly_apply_c1"
+    cpu = line["cpu_baseline"]
+    assert cpu["value"] == line["value"] and cpu["kind"] == "port" and cpu["cores"] >= 1
+    assert cpu["unit"] == "RHS/s" and cpu["sample"]
+    assert line["e2e"] == {"value": line["value"], "unit": "RHS/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_runs_on_rank_zero_only():
+    r = _bench(["--impl", "reference", "--config", "c1", "--steps", "1", "--warmup", "3"],
+               RANK="1", WORLD_SIZE="2")
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.strip() == ""
+
+
+def test_batched_reference_arm_is_unavailable():
+    r = _bench(["--impl", "reference", "--config", "c3s", "--steps", "1", "--warmup", "3"])
+    assert r.returncode == 0, r.stderr
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unavailable"]
