@@ -4,8 +4,8 @@ This module restates, on the CPU and in FP64, the reference library's
 algorithm for the multilevel butterfly factorization of the 2-D Helmholtz
 kernel and its application to vectors.  Only ``tests/``,
 ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg may import
-it, and only as the checker (or the timed CPU baseline) -- never as the
-product path.
+it, and only as the correctness reference (or the timed CPU baseline) --
+never as the product path.
 
 Parity pin: the restatement is checked against the reference library itself
 (``oracle/build_ref.sh`` compiles the reference's own sources into

@@ -1,8 +1,8 @@
 /* Test infrastructure: CPU oracle helpers for the butterfly Helmholtz path.
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
- * this library, and only as the checker or the timed CPU baseline; the
- * product never calls it.
+ * this library, and only as the correctness reference or the timed CPU
+ * baseline; the product never calls it.
  *
  * 1. Kernel matrices restating helm2.c:93-280 with the reference's own
  *    Bessel functions: bf_H0(x) = j0(x) + i y0(x), bf_H1(x) = j1(x) + i y1(x)

@@ -193,8 +193,8 @@ def test_dense_rows_on_gpu_match_oracle(ctx):
 
 
 def test_tolerance_and_leaf_options_against_dense(ctx):
-    """BASELINE-style knobs (leaf size, rank tolerance, relative pseudo-
-    inverse cut) trade accuracy for size; the result is judged against the
+    """The workloads' knobs (leaf size, rank tolerance, relative pseudo-
+    inverse cut) trade accuracy for size; the result is checked against the
     dense FP64 product."""
     src = O.uniform_square_points(4096, 0)
     tgt = O.curve_points("circle", 4096)
