@@ -127,6 +127,8 @@ def lib() -> ctypes.CDLL:
         "bfgPlanHelm2": [ctypes.c_double, _VP, _I64, _VP, _I64, ctypes.POINTER(_FacOptionsC),
                          _VP, _VP, ctypes.c_char_p, _I64, ctypes.POINTER(_I64)],
         "bfgBessel01Host": [_VP, _I64, _VP],
+        "bfgPlanCheckApply": [_VP, _I64, _VP, _VP, _VP, _VP, ctypes.POINTER(_FacOptionsC),
+                              ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64, _VP],
         "bfgFacPrepare": [_VP, ctypes.c_int32],
         "bfgFacAutotune": [_VP, ctypes.c_int32, _I64, _VP, ctypes.c_int32,
                            ctypes.POINTER(ctypes.c_int32)],
@@ -566,6 +568,33 @@ def plan_helm2(k: float, src, tgt, leaf_size: int = 1, rank_eps: float = 1e-15):
     if st != BFG_OK:
         raise BfgError(st, "plan_helm2 failed")
     return sp, tp, buf.value.decode()
+
+
+def check_apply_schedule(problems, leaf_size: int = 1, rank_eps: float = 1e-15, rhs: int = 4,
+                         ctas: int = 152, seed: int = 1):
+    """Host-only self-check of the apply's work decomposition
+    (bfgPlanCheckApply), no GPU involved.  problems: a list of (k, src, tgt)
+    planned as one factorization (one problem) or a batched one.  Returns
+    (staged-program difference, worst chunk-schedule difference), each the
+    relative Frobenius distance from a direct evaluation of the plan's
+    structure on seeded block values."""
+    ks = np.array([float(p[0]) for p in problems], dtype=np.float64)
+    srcs = [_xy(p[1]) for p in problems]
+    tgts = [_xy(p[2]) for p in problems]
+    so = np.concatenate([[0], np.cumsum([len(a) for a in srcs])]).astype(np.int64)
+    to = np.concatenate([[0], np.cumsum([len(a) for a in tgts])]).astype(np.int64)
+    src = np.ascontiguousarray(np.concatenate(srcs))
+    tgt = np.ascontiguousarray(np.concatenate(tgts))
+    opts = _FacOptionsC()
+    lib().bfgFacOptionsDefault(ctypes.byref(opts))
+    opts.leafSize, opts.rankEps = int(leaf_size), float(rank_eps)
+    err = np.zeros(2, dtype=np.float64)
+    st = lib().bfgPlanCheckApply(_ptr(ks), len(problems), _ptr(src), _ptr(so), _ptr(tgt),
+                                 _ptr(to), ctypes.byref(opts), int(rhs), int(ctas), int(seed),
+                                 _ptr(err))
+    if st != BFG_OK:
+        raise BfgError(st, "check_apply_schedule failed")
+    return float(err[0]), float(err[1])
 
 
 def quadtree_build(point_sets, leaf_size: int = 1, on_gpu: bool = False,

@@ -23,7 +23,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
           "-I" + os.path.join(ROOT, "include")]
 SOURCES = ["bfg_kernels.cu", "bfg_plan.cpp", "bfg_api.cpp", "bfg_noalloc.cu", "bfg_solver.cu",
-           "bfg_tc.cu", "bfg_tree.cu", "bfg_df64.cu", "bfg_mlp.cu", "bfg_mlp_api.cpp"]
+           "bfg_tc.cu", "bfg_tree.cu", "bfg_df64.cu", "bfg_mlp.cu", "bfg_mlp_api.cpp",
+           "bfg_check.cpp"]
 
 
 def nvcc() -> str:

@@ -1302,9 +1302,7 @@ bfgStatus bfgFacAutotune(bfgFac f, bfgPrecision prec, int64_t R, double *stageMs
     bfg::makeApplyProgram(f->plan, p128, bfg::kTcRows);
     size_t const nStages = tc.stages;
     int32_t const ctas = tc.ctas;
-    // candidate cost models: the default first
-    std::vector<bfg::TcCostModel> models = {
-        {60, 1, 29}, {40, 1, 29}, {90, 1, 29}, {60, 3, 29}, {60, 0, 29}, {60, 1, 60}, {0, 0, 100}};
+    std::vector<bfg::TcCostModel> const models = bfg::tcCandidateModels();   // default first
     size_t const K = models.size();
     std::vector<bfg::TcSchedule> cands(K);
     for (size_t k = 0; k < K; ++k) {

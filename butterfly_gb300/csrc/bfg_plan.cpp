@@ -888,6 +888,10 @@ void makeApplyProgram(Plan const &plan, ApplyProgram &prog, int itemRows) {
   }
 }
 
+std::vector<TcCostModel> tcCandidateModels() {
+  return {{60, 1, 29}, {40, 1, 29}, {90, 1, 29}, {60, 3, 29}, {60, 0, 29}, {60, 1, 60}, {0, 0, 100}};
+}
+
 void makeTcSchedule(ApplyProgram const &prog, int terms, int ctas, TcSchedule &sc,
                     TcCostModel const &model) {
   sc = TcSchedule();

@@ -257,6 +257,8 @@ struct TcCostModel {
 // model gives the same tiles.
 void makeTcSchedule(ApplyProgram const &prog128, int terms, int ctas, TcSchedule &sched,
                     TcCostModel const &model = TcCostModel());
+// the cost models the autotuner times, the default first
+std::vector<TcCostModel> tcCandidateModels();
 
 // Fill descriptors for the kernel-evaluation and re-expansion kernels.
 struct FillDesc {

@@ -396,6 +396,26 @@ bfgStatus bfgPlanHelm2(double k, double const *srcXy, int64_t numSrc,
                        int64_t *tgtPerm, char *buf, int64_t capacity,
                        int64_t *length);
 
+/* Host-only self-check of the apply's work decomposition (no GPU; no
+ * counterpart in the reference).  Plans these inputs as
+ * bfgFacHelm2MakeMultilevel (numProblems = 1) or bfgFacHelm2MakeBatched
+ * would, gives every stored block seeded pseudo-random entries and
+ * evaluates A X for numRhs (1..64) seeded right-hand sides three ways in
+ * FP64 on the host: from the plan's block structure directly, by the staged
+ * program the device kernels execute (items, workspace regions, final sum),
+ * and by the tensor-core chunk schedules dealt to `ctas` persistent CTAs
+ * under every cost model bfgFacAutotune tries.  relErr[0] receives the
+ * relative Frobenius difference of the staged program from the direct
+ * evaluation, relErr[1] the largest over the chunk schedules.  A schedule
+ * that reads a workspace row no earlier stage wrote gives a non-finite
+ * difference; one that writes a row twice in a stage, or whose chunks do
+ * not form whole items, returns BFG_ERROR_RUNTIME.  Only a difference is
+ * returned, never an operator value. */
+bfgStatus bfgPlanCheckApply(double const *k, int64_t numProblems, double const *srcXy,
+                            int64_t const *srcOffsets, double const *tgtXy,
+                            int64_t const *tgtOffsets, bfgFacOptions const *opts,
+                            int32_t numRhs, int32_t ctas, uint64_t seed, double *relErr);
+
 /* A quadtree node (BfQuadtreeNode, quadtree_node.h:22-39): bounding box,
  * split point, the node's points as a range of the tree order, children in
  * quadrant order (quadtree_node.h:31-37). */
