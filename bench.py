@@ -205,7 +205,9 @@ def max_over_ranks(v, dist):
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    # NCCL reduces device tensors, gloo (the CPU test backend) host ones
+    dev = "cpu" if dist.get_backend() == "gloo" else "cuda"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
