@@ -496,12 +496,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
         if (i + 2 < nCh && !bulkOf(d2)) issueX(d2, i + 2);
         cpAsyncCommit();
         // bulk inputs land on fullX, which the producer arrives on only once
-        // the MMAs of chunk i-S are done; the empty wait then returns at once
-        if (bulkOf(d0) && !mbarWait(fullX + 8 * s, (uint32_t)((i / S) & 1), abortFlag)) {
+        // the MMAs of chunk i-S are done; the empty wait then returns at once.
+        // A warp gives up as one (a vote): were a phase to complete while
+        // the abort flag is being set, some lanes could pass the wait and
+        // others leave the loop, and the passing lanes' __syncwarp would
+        // then wait forever for lanes already at the final barrier.
+        if (bulkOf(d0) &&
+            !__all_sync(0xffffffffu, mbarWait(fullX + 8 * s, (uint32_t)((i / S) & 1), abortFlag))) {
           *abortFlag = 1;
           break;
         }
-        if (i >= S && !mbarWait(empty + 8 * s, (uint32_t)((i / S - 1) & 1), abortFlag)) {
+        if (i >= S &&
+            !__all_sync(0xffffffffu,
+                        mbarWait(empty + 8 * s, (uint32_t)((i / S - 1) & 1), abortFlag))) {
           *abortFlag = 1;
           break;
         }
@@ -567,7 +574,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
         Ce const d = dn;
         dn = loadCe(j + 1);
         int const b = (int)(j & 1);
-        if (!mbarWait(accFull + 8 * b, (uint32_t)((j >> 1) & 1), abortFlag)) {
+        // as one warp (a vote), for the collective TMEM loads below
+        if (!__all_sync(0xffffffffu, mbarWait(accFull + 8 * b, (uint32_t)((j >> 1) & 1), abortFlag))) {
           *abortFlag = 1;
           break;
         }
