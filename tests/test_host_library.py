@@ -133,3 +133,20 @@ def test_ctypes_structs_match_header(tmp_path):
                     str(exe)], check=True)
     got = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
     assert [g for g in got if g] == want
+
+
+@pytest.mark.parametrize("config", ["c2", "c4"])
+def test_product_plan_matches_oracle_at_benchmark_sizes(config):
+    """The benchmark workloads' plans (c2: 65,536 points, k = 512; c4, the
+    metric's 256-RHS target: 262,144 points on the star, k = 2,048) from the
+    library's planner and the oracle's, point for point and block for block."""
+    import bench
+    cfg = bench.CONFIGS[config]
+    src = O.uniform_square_points(cfg["n"], 0)
+    tgt = O.curve_points(cfg["curve"], cfg["n"], cfg["a"], cfg["b"])
+    sp, tp, txt = B.plan_helm2(cfg["k"], src, tgt, leaf_size=cfg["leaf"], rank_eps=cfg["tol"])
+    fac = O.Factorization(O.Helm2(cfg["k"]), src, tgt, leaf_size=cfg["leaf"], eps=cfg["tol"],
+                          fill=False)
+    assert np.array_equal(sp, fac.src_perm)
+    assert np.array_equal(tp, fac.tgt_perm)
+    assert txt == fac.plan_text()
