@@ -68,3 +68,13 @@ def test_bad_arguments_are_refused():
     bad[3, 0] = np.nan
     with pytest.raises(B.BfgError):
         B.check_apply_schedule([(10.0, bad, tgt)])
+
+
+def test_benchmark_workload():
+    """The headline workload's plan (65,536 points, k = 512, leaf 64, 1e-10)
+    with one CTA per SM: the schedules the benchmark times (about 11 s)."""
+    import bench
+    cfg = bench.CONFIGS["c2"]
+    src = B.uniform_square_points(cfg["n"], 0)
+    tgt = B.curve_points(cfg["curve"], cfg["n"], cfg["a"], cfg["b"])
+    _check([(cfg["k"], src, tgt)], leaf_size=cfg["leaf"], rank_eps=cfg["tol"], rhs=1, ctas=152)
