@@ -78,3 +78,13 @@ def test_benchmark_workload():
     src = B.uniform_square_points(cfg["n"], 0)
     tgt = B.curve_points(cfg["curve"], cfg["n"], cfg["a"], cfg["b"])
     _check([(cfg["k"], src, tgt)], leaf_size=cfg["leaf"], rank_eps=cfg["tol"], rhs=1, ctas=152)
+
+
+def test_batched_benchmark_workload():
+    """The batched workload at 64 problems (N log-uniform in [1,024, 4,096],
+    k = N / 30, leaf 64, 1e-8): one plan with a root per problem (16 s)."""
+    import bench
+    cfg = bench.CONFIGS["c3s"]
+    _, probs, ks = bench.batched_problems(B, cfg)
+    _check([(k, s, t) for k, (s, t) in zip(ks, probs)], leaf_size=cfg["leaf"],
+           rank_eps=cfg["tol"], rhs=2, ctas=152)
