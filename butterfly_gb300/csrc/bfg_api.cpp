@@ -56,6 +56,32 @@ void ck(cudaError_t e, char const *what) {
     throw BfgError{BFG_ERROR_CUDA, std::string(what) + ": " + cudaGetErrorString(e)};
 }
 
+// CUDA events released on every exit path, a failed check included
+struct Events {
+  std::vector<cudaEvent_t> v;
+  Events(size_t n, char const *what) : v(n, nullptr) {
+    for (auto &e : v) {
+      cudaError_t const r = cudaEventCreate(&e);
+      if (r != cudaSuccess) {
+        e = nullptr;
+        release();
+        ck(r, what);
+      }
+    }
+  }
+  ~Events() { release(); }
+  Events(Events const &) = delete;
+  Events &operator=(Events const &) = delete;
+  cudaEvent_t operator[](size_t i) const { return v[i]; }
+  void release() {
+    for (auto &e : v)
+      if (e) {
+        cudaEventDestroy(e);
+        e = nullptr;
+      }
+  }
+};
+
 template <typename T>
 void upload(DevBuf &buf, std::vector<T> const &v, cudaStream_t s, char const *what) {
   size_t n = std::max<size_t>(1, v.size()) * sizeof(T);
@@ -290,11 +316,8 @@ void factorize(bfgFac f) {
   ck(status.ensure(sizeof(int32_t)), "status");
   ck(cudaMemsetAsync(status.p, 0, sizeof(int32_t), s), "status");
 
-  cudaEvent_t e0, e1, eFill, eSmem;
-  ck(cudaEventCreate(&e0), "event");
-  ck(cudaEventCreate(&e1), "event");
-  ck(cudaEventCreate(&eFill), "event");
-  ck(cudaEventCreate(&eSmem), "event");
+  Events const ev(4, "event");
+  cudaEvent_t const e0 = ev[0], e1 = ev[1], eFill = ev[2], eSmem = ev[3];
   ck(cudaEventRecord(e0, s), "event");
 
   bfg::KernelParams kpTrue = kernelParams(f->helm, f->helm.layerPot);
@@ -366,10 +389,6 @@ void factorize(bfgFac f) {
   cudaEventElapsedTime(&msFill, e0, eFill);
   cudaEventElapsedTime(&msSmem, eFill, eSmem);
   cudaEventElapsedTime(&msGlobal, eSmem, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  cudaEventDestroy(eFill);
-  cudaEventDestroy(eSmem);
   f->stats.fillMs = msFill;
   f->stats.reexpSmemMs = msSmem;
   f->stats.reexpGlobalMs = msGlobal;
@@ -1202,14 +1221,12 @@ bfgStatus bfgFacApplyTimed(bfgFac f, bfgPrecision prec, void const *X, int64_t l
     *numLaunches = (int32_t)n;
     if (!ms || cap < (int32_t)n) return fail(f->ctx, BFG_ERROR_OUT_OF_RANGE, "timed apply: buffer too small");
     preparePrecision(f, prec);
-    std::vector<cudaEvent_t> ev(n + 1);
-    for (auto &e : ev) ck(cudaEventCreate(&e), "event");
-    bfgStatus st = applyDispatch(f, prec, X, ldx, R, Y, ldy, flags, &ev);
+    Events ev(n + 1, "event");
+    bfgStatus st = applyDispatch(f, prec, X, ldx, R, Y, ldy, flags, &ev.v);
     if (st == BFG_OK) {
       ck(cudaEventSynchronize(ev[n]), "event");
       for (size_t i = 0; i < n; ++i) cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);
     }
-    for (auto &e : ev) cudaEventDestroy(e);
     if (st == BFG_OK && isTcPrecision(prec)) checkTcStatus(f);
     return st;
   });
@@ -1316,8 +1333,7 @@ bfgStatus bfgFacAutotune(bfgFac f, bfgPrecision prec, int64_t R, double *stageMs
     ck(xs.ensure((size_t)std::max<int64_t>(1, p.numCols) * R * sizeof(float2)), "autotune");
     ck(cudaMemsetAsync(xs.p, 0, (size_t)p.numCols * R * sizeof(float2), s), "autotune");
     ck(f->ws.ensure((size_t)std::max<int64_t>(1, p.wsRows) * R * sizeof(float2)), "workspace");
-    std::vector<cudaEvent_t> ev(nStages + 1);
-    for (auto &e : ev) ck(cudaEventCreate(&e), "autotune");
+    Events const ev(nStages + 1, "autotune");
     int const reps = 5;
     std::vector<std::vector<float>> best(K, std::vector<float>(nStages, 1e30f));
     DevBuf dch, dc0;
@@ -1343,7 +1359,6 @@ bfgStatus bfgFacAutotune(bfgFac f, bfgPrecision prec, int64_t R, double *stageMs
         }
       }
     }
-    for (auto &e : ev) cudaEventDestroy(e);
     checkTcStatus(f);
     // per stage the fastest candidate, spliced into one schedule
     std::vector<bfg::TcChunk> chunks;
