@@ -49,7 +49,7 @@ class _FacOptionsC(ctypes.Structure):
     _fields_ = [("leafSize", ctypes.c_int64), ("rankEps", ctypes.c_double),
                 ("pinvCut", ctypes.c_int32), ("treeOnGpu", ctypes.c_int32),
                 ("pinvTol", ctypes.c_double), ("jacobiArith", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("sketch", ctypes.c_int32)]
 
 
 class _QuadtreeNodeC(ctypes.Structure):
@@ -71,7 +71,10 @@ class _FacStatsC(ctypes.Structure):
         "numRows", "numCols", "numBlocks", "numFirst", "numMiddle", "numLast",
         "numDense", "numProducts", "arenaEntries", "numStages", "numItems",
         "maxRank", "jacobiNotConverged")] + [(n, ctypes.c_double) for n in (
-            "factorMs", "flopsPerRhs", "fillMs", "reexpSmemMs", "reexpGlobalMs")]
+            "factorMs", "flopsPerRhs", "fillMs", "reexpSmemMs", "reexpGlobalMs")] + [
+        (n, ctypes.c_int64) for n in (
+            "numSketched", "sketchRetries", "sketchFallbacks", "sketchMaxWidth")] + [
+        (n, ctypes.c_double) for n in ("sketchMs", "sketchMeanWidth")]
 
 
 class _RngC(ctypes.Structure):
@@ -286,7 +289,7 @@ class FacHelm2:
     def make_multilevel(helm: Helm2, src_tree: Quadtree, tgt_tree: Quadtree | None = None,
                         *, rank_eps: float = 1e-15, pinv_tol: float | None = None,
                         tree_on_gpu: bool = False, jacobi: str = "fp64",
-                        context: Context | None = None) -> "Fac":
+                        sketch: bool = True, context: Context | None = None) -> "Fac":
         tgt_tree = src_tree if tgt_tree is None else tgt_tree
         if src_tree.leaf_size != tgt_tree.leaf_size:
             raise ValueError("both trees must use the same leaf size")
@@ -299,6 +302,7 @@ class FacHelm2:
         opts.rankEps = float(rank_eps)
         opts.treeOnGpu = 1 if tree_on_gpu else 0
         opts.jacobiArith = {"fp64": 0, "df64": 1}[jacobi]
+        opts.sketch = 1 if sketch else 0
         if pinv_tol is not None:
             opts.pinvCut, opts.pinvTol = 1, float(pinv_tol)
         h = _VP()
@@ -311,7 +315,7 @@ class FacHelm2:
 
 def make_batched(helm: Helm2, problems, ks, *, leaf_size: int = 1, rank_eps: float = 1e-15,
                  pinv_tol: float | None = None, context: Context | None = None,
-                 tree_on_gpu: bool = False, jacobi: str = "fp64") -> "Fac":
+                 tree_on_gpu: bool = False, jacobi: str = "fp64", sketch: bool = True) -> "Fac":
     """Factorize many independent problems in one go (bfgFacHelm2MakeBatched).
     ``problems``: list of (src, tgt) or (src, tgt, src_normals, tgt_normals);
     ``ks``: wavenumber per problem.  The result applies diag(A_0, ..., A_P-1);
@@ -336,6 +340,7 @@ def make_batched(helm: Helm2, problems, ks, *, leaf_size: int = 1, rank_eps: flo
     opts.rankEps = float(rank_eps)
     opts.treeOnGpu = 1 if tree_on_gpu else 0
     opts.jacobiArith = {"fp64": 0, "df64": 1}[jacobi]
+    opts.sketch = 1 if sketch else 0
     if pinv_tol is not None:
         opts.pinvCut, opts.pinvTol = 1, float(pinv_tol)
     h = _VP()

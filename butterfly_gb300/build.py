@@ -3,7 +3,7 @@
     python -m butterfly_gb300.build          # or __graft_entry__.build()
 
 Translation units compile in parallel into butterfly_gb300/_build/ and link
-into butterfly_gb300/libbfg.so (CUDA runtime linked statically).
+into butterfly_gb300/libbfg.so (CUDA runtime linked shared).
 """
 from __future__ import annotations
 
@@ -24,7 +24,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
           "-I" + os.path.join(ROOT, "include")]
 SOURCES = ["bfg_kernels.cu", "bfg_plan.cpp", "bfg_api.cpp", "bfg_noalloc.cu", "bfg_solver.cu",
            "bfg_tc.cu", "bfg_tree.cu", "bfg_df64.cu", "bfg_mlp.cu", "bfg_mlp_api.cpp",
-           "bfg_check.cpp"]
+           "bfg_check.cpp", "bfg_sketch.cu"]
 
 
 def nvcc() -> str:

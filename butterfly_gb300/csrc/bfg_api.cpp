@@ -252,6 +252,8 @@ bfg::FillDesc toDesc(bfg::Block const &b) {
   d.ceq[0] = b.ceq.cx; d.ceq[1] = b.ceq.cy; d.ceq[2] = b.ceq.r;
   d.cchk[0] = b.cchk.cx; d.cchk[1] = b.cchk.cy; d.cchk[2] = b.cchk.r;
   d.k = b.k;
+  d.j0 = 0;
+  d.nTot = b.n;
   return d;
 }
 
@@ -263,6 +265,25 @@ constexpr double kDfJacobiMinCut = 1e-10;
 constexpr int64_t kScratchBudgetEntries = (int64_t)1 << 27;   // 2 GiB of complex128
 // ranks from which a block that misses shared memory gets a whole cluster
 constexpr int32_t kClusterMinRank = 128;
+// the randomized re-expansion path: blocks from this rank estimate whose
+// initial sketch is at most kSketchMaxFraction of it; the sketch width is
+// kSketchWidthScale k r1 r2 / R + kSketchWidthPad; scratch per batch
+constexpr int32_t kSketchMinRank = 256;
+constexpr double kSketchMaxFraction = 0.6;
+constexpr double kSketchWidthScale = 1.15;
+constexpr int32_t kSketchWidthPad = 48;
+constexpr int64_t kSketchBudgetEntries = (int64_t)1 << 30;   // 16 GiB of complex128
+// LAST and DENSE blocks are filled in column pieces of at most this many
+// columns and entries, so that one large block spreads over many CTAs
+constexpr int32_t kFillPieceCols = 2048;
+constexpr int64_t kFillPieceEntries = (int64_t)1 << 20;
+
+// the sketch's capture threshold: its smallest singular value must lie
+// below this fraction of the largest, three decades under the relative cut
+// and never closer than 1e-13 to the kernels' rounding floor (~1e-14)
+double sketchCapture(bfgFacOptions const &o) {
+  return std::max(1e-13, std::min(1e-12, 1e-3 * o.pinvTol));
+}
 
 void factorize(bfgFac f) {
   cudaStream_t s = f->ctx->stream;
@@ -278,29 +299,64 @@ void factorize(bfgFac f) {
   // memory (8 or 16 warps), global memory with one CTA, or global memory
   // with a thread-block cluster for the largest ranks (the critical path)
   std::vector<bfg::FillDesc> fill, reSmem8, reSmem16, reGlobal, reCluster;
+  std::vector<bfg::SketchInput> sketch;
   int32_t maxProxyN = 1;
   int64_t maxRank = 0;
-  for (auto const &b : plan.blocks) {
-    bfg::FillDesc d = toDesc(b);
-    if (b.kind == bfg::kLast || b.kind == bfg::kDense) {
-      fill.push_back(d);
-      if (b.kind == bfg::kLast) maxProxyN = std::max(maxProxyN, b.n);
-      if (b.kind == bfg::kLast) maxRank = std::max<int64_t>(maxRank, b.n);
-      continue;
-    }
-    maxRank = std::max<int64_t>(maxRank, b.m);
-    if (bfg::reexpansionGeoBytes(b.m, b.n) > kSmemLimit)
-      throw BfgError{BFG_ERROR_NOT_IMPLEMENTED, "block geometry exceeds shared memory"};
-    if (b.m <= 16 && bfg::reexpansionSmemBytes(b.m, b.n, 8) <= kSmemLimit)
+  bool const sketchCut = f->opts.pinvCut == 1 && f->opts.pinvTol >= kDfJacobiMinCut;
+  auto route = [&](bfg::FillDesc const &d) {
+    if (d.m <= 16 && bfg::reexpansionSmemBytes(d.m, d.n, 8) <= kSmemLimit)
       reSmem8.push_back(d);
-    else if (bfg::reexpansionSmemBytes(b.m, b.n, 16) <= kSmemLimit)
+    else if (bfg::reexpansionSmemBytes(d.m, d.n, 16) <= kSmemLimit)
       reSmem16.push_back(d);
-    else if (b.m >= kClusterMinRank)
+    else if (d.m >= kClusterMinRank)
       reCluster.push_back(d);
     else
       reGlobal.push_back(d);
+  };
+  for (auto const &b : plan.blocks) {
+    bfg::FillDesc d = toDesc(b);
+    if (b.kind == bfg::kLast || b.kind == bfg::kDense) {
+      if (b.kind == bfg::kLast) maxRank = std::max<int64_t>(maxRank, b.n);
+      // column pieces (the proxy points of a LAST piece come from j0 / nTot)
+      int64_t const w = std::max<int64_t>(
+          1, std::min<int64_t>(kFillPieceCols, kFillPieceEntries / std::max(1, b.m)));
+      for (int64_t j = 0; j < b.n; j += w) {
+        bfg::FillDesc q = d;
+        q.n = (int32_t)std::min<int64_t>(w, b.n - j);
+        q.arenaOff = d.arenaOff + j * b.m;
+        if (b.kind == bfg::kLast) {
+          q.j0 = (int32_t)j;
+          q.nTot = b.n;
+          maxProxyN = std::max(maxProxyN, q.n);
+        } else {
+          q.s0 = d.s0 + j;
+          q.j0 = 0;
+          q.nTot = q.n;
+        }
+        fill.push_back(q);
+      }
+      continue;
+    }
+    maxRank = std::max<int64_t>(maxRank, b.m);
+    bool const fullOk = bfg::reexpansionGeoBytes(b.m, b.n) <= kSmemLimit;
+    if (f->opts.sketch && sketchCut && b.m >= kSketchMinRank) {
+      int32_t const l = bfg::sketchWidth(d, kSketchWidthScale, kSketchWidthPad);
+      if (l <= kSketchMaxFraction * b.m) {
+        sketch.push_back(bfg::SketchInput{d, l, fullOk ? 1 : 0});
+        continue;
+      }
+    }
+    if (!fullOk) {
+      if (!f->opts.sketch)
+        throw BfgError{BFG_ERROR_NOT_IMPLEMENTED,
+                       "block geometry exceeds shared memory (options.sketch = 0)"};
+      // the randomized path with the capture test, or at full width
+      int32_t const l = sketchCut ? bfg::sketchWidth(d, kSketchWidthScale, kSketchWidthPad) : b.m;
+      sketch.push_back(bfg::SketchInput{d, l, 0});
+      continue;
+    }
+    route(d);
   }
-  if (maxProxyN > 6000) throw BfgError{BFG_ERROR_NOT_IMPLEMENTED, "rank above 6000"};
   // largest Jacobi first, so that the longest CTAs start in the first wave
   auto cost = [](bfg::FillDesc const &d) {
     return (double)d.m * d.m * (3.0 * d.m + d.n);
@@ -316,8 +372,8 @@ void factorize(bfgFac f) {
   ck(status.ensure(sizeof(int32_t)), "status");
   ck(cudaMemsetAsync(status.p, 0, sizeof(int32_t), s), "status");
 
-  Events const ev(4, "event");
-  cudaEvent_t const e0 = ev[0], e1 = ev[1], eFill = ev[2], eSmem = ev[3];
+  Events const ev(5, "event");
+  cudaEvent_t const e0 = ev[0], e1 = ev[1], eFill = ev[2], eSmem = ev[3], eSketch = ev[4];
   ck(cudaEventRecord(e0, s), "event");
 
   bfg::KernelParams kpTrue = kernelParams(f->helm, f->helm.layerPot);
@@ -330,6 +386,25 @@ void factorize(bfgFac f) {
                            arena, maxProxyN, st, s),
      "fill kernel");
   ck(cudaEventRecord(eFill, s), "event");
+
+  // the randomized re-expansions; blocks it hands back join the full path
+  {
+    std::vector<bfg::FillDesc> back;
+    bfg::SketchReport rep;
+    ck(bfg::runSketchReexpansion(sketch, src, kpProxy, f->opts.pinvCut, f->opts.pinvTol,
+                                 sketchCapture(f->opts), arena, kSketchBudgetEntries, s, &back,
+                                 &rep),
+       "randomized re-expansion");
+    for (auto const &d : back) route(d);
+    f->stats.numSketched = rep.blocks;
+    f->stats.sketchRetries = rep.retries;
+    f->stats.sketchFallbacks = rep.fallbacks;
+    f->stats.sketchMaxWidth = rep.maxWidth;
+    f->stats.sketchMs = rep.ms;
+    f->stats.sketchMeanWidth = rep.blocks ? (double)rep.sumWidth / (double)rep.blocks : 0.0;
+    if (rep.notConverged) f->stats.jacobiNotConverged = 1;
+  }
+  ck(cudaEventRecord(eSketch, s), "event");
 
   auto maxBytes = [](std::vector<bfg::FillDesc> const &v, int warps, bool geoOnly) {
     int64_t m = 0;
@@ -387,7 +462,7 @@ void factorize(bfgFac f) {
   float ms = 0, msFill = 0, msSmem = 0, msGlobal = 0;
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventElapsedTime(&msFill, e0, eFill);
-  cudaEventElapsedTime(&msSmem, eFill, eSmem);
+  cudaEventElapsedTime(&msSmem, eSketch, eSmem);
   cudaEventElapsedTime(&msGlobal, eSmem, e1);
   f->stats.fillMs = msFill;
   f->stats.reexpSmemMs = msSmem;
@@ -398,7 +473,7 @@ void factorize(bfgFac f) {
 
   f->stats.factorMs = ms;
   f->stats.maxRank = maxRank;
-  f->stats.jacobiNotConverged = (hst & bfg::kStatusJacobiNotConverged) ? 1 : 0;
+  if (hst & bfg::kStatusJacobiNotConverged) f->stats.jacobiNotConverged = 1;
 }
 
 void buildApply(bfgFac f) {
@@ -822,6 +897,7 @@ void bfgFacOptionsDefault(bfgFacOptions *o) {
   o->rankEps = 1e-15;
   o->pinvCut = 0;
   o->pinvTol = 0.0;
+  o->sketch = 1;
 }
 
 bfgStatus bfgFacHelm2MakeMultilevel(bfgContext ctx, bfgHelm2 const *helm, double const *srcXy,
@@ -844,6 +920,7 @@ bfgStatus bfgFacHelm2MakeMultilevel(bfgContext ctx, bfgHelm2 const *helm, double
     bfgFacOptionsDefault(&o);
     if (opts) o = *opts;
     if (o.leafSize < 1 || !(o.rankEps > 0 && o.rankEps < 1) || (o.pinvCut != 0 && o.pinvCut != 1) || (o.jacobiArith != 0 && o.jacobiArith != 1) ||
+        (o.sketch != 0 && o.sketch != 1) ||
         (o.jacobiArith == 1 && !(o.pinvCut == 1 && o.pinvTol >= kDfJacobiMinCut)) ||
         (o.pinvCut == 1 && !(o.pinvTol > 0 && o.pinvTol < 1)))
       return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "make: bad options");
@@ -926,6 +1003,7 @@ bfgStatus bfgFacHelm2MakeBatched(bfgContext ctx, bfgHelm2 const *helm, double co
     bfgFacOptionsDefault(&o);
     if (opts) o = *opts;
     if (o.leafSize < 1 || !(o.rankEps > 0 && o.rankEps < 1) || (o.pinvCut != 0 && o.pinvCut != 1) || (o.jacobiArith != 0 && o.jacobiArith != 1) ||
+        (o.sketch != 0 && o.sketch != 1) ||
         (o.jacobiArith == 1 && !(o.pinvCut == 1 && o.pinvTol >= kDfJacobiMinCut)) ||
         (o.pinvCut == 1 && !(o.pinvTol > 0 && o.pinvTol < 1)))
       return fail(ctx, BFG_ERROR_INVALID_ARGUMENTS, "batched make: bad options");

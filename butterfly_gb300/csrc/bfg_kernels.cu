@@ -25,6 +25,7 @@
 #include <cstdlib>
 #include <cstring>
 
+#include "bfg_device.cuh"
 #include "bfg_kernels.cuh"
 #include "hankel.cuh"
 
@@ -35,50 +36,6 @@ namespace {
 constexpr double kTwoPiD = 6.283185307179586;   // const.h BF_TWO_PI
 constexpr double kEps = 2.220446049250313e-16;
 constexpr int kMaxSweeps = 60;
-
-__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
-  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-
-// Kernel value K(x_tgt, x_src) for the layer potential in kp (helm2.c:38-91;
-// matrix fills return 0 at r == 0, helm2.c:114, 159-160, 207, 255).
-__device__ __forceinline__ double2 kernelValue(KernelParams const &kp, double tx,
-                                               double ty, double tnx, double tny,
-                                               double sx, double sy, double snx,
-                                               double sny) {
-  double const r = hypot(sx - tx, sy - ty);
-  if (r == 0.0) return make_double2(0.0, 0.0);
-  double const kr = kp.k * r;
-  if (kp.layerPot == kLpSingle) {
-    Bessel01 b = bessel01<false>(kr);
-    return make_double2(-0.25 * b.y0, 0.25 * b.j0);          // (i/4) H0
-  }
-  Bessel01 b = bessel01<true>(kr);
-  // (i/4) k H1(kr) / r = (k/(4r)) (-Y1 + i J1)
-  double const f = 0.25 * kp.k / r;
-  double2 const scale = make_double2(-f * b.y1, f * b.j1);
-  if (kp.layerPot == kLpPvDouble) {
-    double const dot = snx * (tx - sx) + sny * (ty - sy);
-    return make_double2(scale.x * dot, scale.y * dot);
-  }
-  if (kp.layerPot == kLpPvNormalDerivSingle) {
-    double const dot = tnx * (tx - sx) + tny * (ty - sy);
-    return make_double2(scale.x * dot, scale.y * dot);
-  }
-  // combined field alpha S + beta D
-  double const dot = snx * (tx - sx) + sny * (ty - sy);
-  double2 const S = make_double2(-0.25 * b.y0, 0.25 * b.j0);
-  double2 const D = make_double2(scale.x * dot, scale.y * dot);
-  double2 const a = cmul(make_double2(kp.alphaRe, kp.alphaIm), S);
-  double2 const c = cmul(make_double2(kp.betaRe, kp.betaIm), D);
-  return make_double2(a.x + c.x, a.y + c.y);
-}
-
-__device__ __forceinline__ double warpSum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
 
 // ---------------------------------------------------------------------------
 // LAST and DENSE blocks
@@ -94,10 +51,10 @@ __global__ void fillBlocksKernel(FillDesc const *__restrict__ descs, PointsDev s
   bool const useSrcN = kp.layerPot == kLpPvDouble || kp.layerPot == kLpCombinedField;
   bool const useTgtN = kp.layerPot == kLpPvNormalDerivSingle;
   if (d.kind == kLast) {
-    double const scale = kTwoPiD / (double)n;
+    double const scale = kTwoPiD / (double)d.nTot;
     for (int b = threadIdx.x; b < n; b += blockDim.x) {
       double s, c;
-      sincos(scale * b, &s, &c);
+      sincos(scale * (d.j0 + b), &s, &c);
       proxy[b] = d.ceq[2] * c + d.ceq[0];
       proxy[n + b] = d.ceq[2] * s + d.ceq[1];
       proxy[2 * n + b] = c;

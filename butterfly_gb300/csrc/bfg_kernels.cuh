@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <vector>
 
 #include "bfg_plan.hpp"
 
@@ -61,6 +62,35 @@ int64_t reexpansionGeoBytes(int32_t m, int32_t n);
 // working on it (threads/32 times the CTAs per block)
 int64_t reexpansionScratchEntries(int32_t m, int32_t warps);
 int32_t reexpansionClusterCtas();
+
+// FIRST/MIDDLE blocks by the randomized range finder (bfg_sketch.cu): one
+// input per block with its initial sketch width l (<= m) and whether the
+// full-Jacobi kernels could take it instead.
+struct SketchInput {
+  FillDesc d;
+  int32_t l;
+  int32_t fullOk;
+};
+struct SketchReport {
+  int64_t blocks = 0;      // blocks computed by this path
+  int64_t retries = 0;     // sketches redone with a wider l
+  int64_t fallbacks = 0;   // blocks handed back to the full path
+  int64_t maxWidth = 0, sumWidth = 0;
+  int32_t notConverged = 0;
+  double ms = 0.0;         // device time of the whole path
+};
+// initial sketch width: widthScale * k r1 r2 / R + widthPad rounded up to 32,
+// at most m (R: distance of the equivalent and check circles' centres)
+int32_t sketchWidth(FillDesc const &d, double widthScale, int32_t widthPad);
+// Computes the blocks of `in` into the arena.  A block whose sketch missed
+// part of Z_equiv's numerical rank (smallest sigma above capture * sigma0) is
+// sketched again with twice the width, or, when that width passes 0.6 m and
+// the full path can take it, appended to *fallback.  Scratch is allocated per
+// batch of blocks within budgetEntries complex entries (at least one block).
+cudaError_t runSketchReexpansion(std::vector<SketchInput> const &in, PointsDev src,
+                                 KernelParams kp, int32_t cutMode, double cutTol, double capture,
+                                 double2 *arena, int64_t budgetEntries, cudaStream_t stream,
+                                 std::vector<FillDesc> *fallback, SketchReport *rep);
 
 // Dense kernel rows: out[s*ldo + r] = sum_j K(t_rows[s], src_j) x[j*ldx + r]
 cudaError_t launchDenseRows(PointsDev src, int64_t nSrc, PointsDev tgt,

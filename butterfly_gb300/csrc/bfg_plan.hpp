@@ -267,6 +267,9 @@ struct FillDesc {
   int64_t s0, t0;               // tree-order point offsets
   double corig[3], ceq[3], cchk[3];
   double k;                     // wavenumber
+  // a LAST block filled in column pieces: this piece holds columns
+  // [j0, j0 + n) of the block's nTot proxy points (arenaOff at column j0)
+  int32_t j0, nTot;
 };
 
 }  // namespace bfg

@@ -95,7 +95,19 @@ typedef struct bfgFacOptions {
                           rounding noise at ~1e-14 of the largest singular
                           value, so it requires pinvCut = 1 with
                           pinvTol >= 1e-10 */
-  int32_t reserved;
+  int32_t sketch;     /* 1 (default): a FIRST/MIDDLE block of rank estimate
+                         p >= 256 whose Z_equiv has a numerical rank well
+                         below p (about k r1 r2 / R against the estimate's
+                         k r1 r2 / (R - r1 - r2)) takes the randomized range
+                         finder instead of the p x p Jacobi SVD, when
+                         pinvCut = 1 and pinvTol >= 1e-10: the same cut on
+                         the same singular values, to within Z_equiv's
+                         rounding floor (~1e-14 sigma0), at a fraction of the
+                         work.  A block too large for the shared-memory
+                         working set of the full path takes it whatever the
+                         cut.  0: the full path only (such blocks are then
+                         refused with BFG_ERROR_NOT_IMPLEMENTED).  No
+                         counterpart in the reference. */
 } bfgFacOptions;
 
 typedef struct bfgFacStats {
@@ -112,6 +124,12 @@ typedef struct bfgFacStats {
   double fillMs;              /* evaluation and dense blocks */
   double reexpSmemMs;         /* re-expansions held in shared memory */
   double reexpGlobalMs;       /* re-expansions held in global memory */
+  int64_t numSketched;        /* re-expansions by the randomized path */
+  int64_t sketchRetries;      /* sketches redone wider (rank not captured) */
+  int64_t sketchFallbacks;    /* blocks handed back to the full path */
+  int64_t sketchMaxWidth;     /* widest accepted sketch */
+  double sketchMs;            /* device time of the randomized path */
+  double sketchMeanWidth;     /* mean accepted sketch width */
 } bfgFacStats;
 
 /* Contexts: one CUDA device and one stream; calls on a context are

@@ -695,6 +695,40 @@ def lstsq_pinv(A: np.ndarray, B: np.ndarray, rcut: str = "reference",
     return VH[:k, :].conj().T @ tmp2
 
 
+def sketch_width(k: float, ceq, cchk, m: int, scale: float = 1.15, pad: int = 48) -> int:
+    """Initial width of the library's randomized re-expansion for a block
+    with rank estimate m: scale * k r1 r2 / R + pad rounded up to 32, at most
+    m (R: distance of the equivalent and check circles' centres).  The rank
+    estimate of helm2.c:14-36 divides by R - r1 - r2 instead."""
+    R = float(np.hypot(ceq[0] - cchk[0], ceq[1] - cchk[1]))
+    est = k * ceq[2] * cchk[2] / R if R > 0 else float(m)
+    w = int(np.ceil((scale * est + pad) / 32.0)) * 32
+    return m if w >= m else max(32, w)
+
+
+def sketch_pinv(A: np.ndarray, B: np.ndarray, width: int, tol: float,
+                seed: int = 0):
+    """The randomized re-expansion the library runs on the GPU, restated with
+    numpy's LAPACK for the CPU checks (test infrastructure): X ~ pinv_cut(A) B
+    with the relative cut sigma_i >= tol sigma_0 (linalg.c:26-36) taken on the
+    singular values of A restricted to the range of a Gaussian sketch
+    A Omega (Halko, Martinsson, Tropp 2011, algorithms 4.1 and 5.1):
+    Q = qr(A Omega), Q2 R2 = qr(A^H Q), R2^H = U S V^H, so A ~ (Q U) S (Q2 V)^H
+    and X = Q2 V diag(w) S U^H Q^H B.  Returns (X, sigma_min / sigma_max), the
+    second being the library's capture test (the sketch reached A's rounding
+    floor when it is tiny)."""
+    p = A.shape[0]
+    rng = np.random.default_rng(seed)
+    om = rng.standard_normal((p, width)) + 1j * rng.standard_normal((p, width))
+    Q, _ = np.linalg.qr(A @ om)
+    Q2, R2 = np.linalg.qr(A.conj().T @ Q)
+    U, S, VH = np.linalg.svd(R2.conj().T)
+    w = np.where(S >= tol * S.max(), 1.0 / S ** 2, 0.0)
+    T = U * S
+    X = Q2 @ (VH.conj().T @ (w[:, None] * (T.conj().T @ (Q.conj().T @ B))))
+    return X, float(S.min() / S.max())
+
+
 class Factorization:
     """The oracle's butterfly factorization: plan + filled blocks."""
 

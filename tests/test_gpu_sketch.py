@@ -1,0 +1,103 @@
+"""The randomized re-expansion path on the GPU (bfg_sketch.cu), through the C
+ABI, against the full-Jacobi path and the CPU oracle.
+
+Workloads: 8,192 sources in [-1,1]^2 and 8,192 targets on the star curve
+r = 3 + 0.5 cos 5 theta at k = 256, leaf 64, tolerance 1e-7 (10 blocks take
+the path); 16,384 points on the ellipse (3, 2) at k = 256, tolerance 1e-10
+(48 blocks).
+
+Bars:
+  * every sketched block solves the re-expansion least squares
+    (helm2.c:321-365) with a residual within 2x (+1e-12) of the oracle's
+    scipy-zgesvd pseudo-inverse of the same block;
+  * the applied operator is within the tolerance's error of dense FP64 rows
+    computed by the oracle (2e-6 at 1e-7, 2e-9 at 1e-10), and within the same
+    bound of the operator the full path builds.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from oracle import bf_oracle as O
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import butterfly_gb300 as B  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return B.default_context(0)
+
+
+def _problem(N, k, curve, tol, ctx, sketch):
+    src = O.uniform_square_points(N, 0)
+    tgt = O.curve_points(curve, N)
+    fac = B.FacHelm2.make_multilevel(B.Helm2(k), B.Quadtree(src, leaf_size=64),
+                                     B.Quadtree(tgt, leaf_size=64), rank_eps=tol,
+                                     pinv_tol=tol, sketch=sketch, context=ctx)
+    return src, tgt, fac
+
+
+def _error_vs_oracle(src, tgt, fac, k, rows_n=256, R=4):
+    sp, tp = fac.perms()
+    X = O.RefRng(11).complex_randn(len(src) * R).reshape(len(src), R)
+    Y = fac.apply(torch.from_numpy(X).cuda()).cpu().numpy()
+    rows = np.linspace(0, len(tgt) - 1, rows_n).astype(np.int64)
+    Yd = O.dense_rows(O.Helm2(k), src[sp], tgt[tp], rows, X)
+    return Y, rel_err(Y[rows], Yd)
+
+
+@pytest.mark.parametrize("N,k,curve,tol,bound,min_sketched", [
+    (8192, 256.0, "star", 1e-7, 2e-6, 8),
+    (16384, 256.0, "ellipse", 1e-10, 2e-9, 40),
+])
+def test_sketched_operator_against_dense_and_full_path(ctx, N, k, curve, tol, bound,
+                                                       min_sketched):
+    src, tgt, fac = _problem(N, k, curve, tol, ctx, True)
+    st = fac.stats()
+    assert st["numSketched"] >= min_sketched
+    assert st["jacobiNotConverged"] == 0
+    Ys, es = _error_vs_oracle(src, tgt, fac, k)
+    _, _, full = _problem(N, k, curve, tol, ctx, False)
+    assert full.stats()["numSketched"] == 0
+    Yf, ef = _error_vs_oracle(src, tgt, full, k)
+    assert fac.describe() == full.describe()
+    assert es < bound and ef < bound
+    assert rel_err(Ys, Yf) < bound
+
+
+def test_sketched_blocks_solve_the_reexpansion_least_squares(ctx):
+    N, k, tol = 8192, 256.0, 1e-7
+    src, tgt, fac = _problem(N, k, "star", tol, ctx, True)
+    of = O.Factorization(O.Helm2(k), src, tgt, leaf_size=64, eps=tol, rcut="relative",
+                         fill=False)
+    tab, ent = fac.blocks()
+    oblocks = of.blocks()
+    assert len(oblocks) == len(tab)
+    h = O.Helm2(k)
+    checked = 0
+    for (kind, m, n, off), ob in zip(tab, oblocks):
+        if kind not in (0, 1) or m < 256:
+            continue
+        if O.sketch_width(k, ob.ceq, ob.cchk, m) > 0.6 * m:
+            continue
+        Z = ent[off:off + m * n].reshape(n, m).T
+        eq_pts, _ = O.circle_points(ob.ceq, m)
+        chk_pts, _ = O.circle_points(ob.cchk, m)
+        if ob.kind == "first":
+            orig = of.src_tree_pts[ob.src_range[0]:ob.src_range[1]]
+        else:
+            orig, _ = O.circle_points(ob.corig, n)
+        Ze = O.kernel_matrix(h, eq_pts, chk_pts)
+        Zo = O.kernel_matrix(h, orig, chk_pts)
+        Xo = O.lstsq_pinv(Ze, Zo, "relative", tol)
+        r_gpu = np.linalg.norm(Ze @ Z - Zo) / np.linalg.norm(Zo)
+        r_ora = np.linalg.norm(Ze @ Xo - Zo) / np.linalg.norm(Zo)
+        assert r_gpu < 2 * r_ora + 1e-12
+        assert rel_err(Z, Xo) < 1e-6
+        checked += 1
+    assert checked == fac.stats()["numSketched"]
