@@ -57,8 +57,13 @@ METRIC = "Butterfly apply RHS/s at 1e-6 rel err vs plain FP64 GPU; GMRES time-to
 # workload (same geometry, kernels and stage structure at twice the size)
 # reports its dominant launch's traffic as this ratio times its own
 # algorithmic bytes
-NCU_DRAM_PER_ALG = {("fp32", 16, 5): [0.7973, 1.0266, 0.9855, 0.7925],
-                    ("bf16x3", 16, 5): [0.8888, 1.0627, 1.0246, 1.0386]}
+NCU_DRAM_PER_ALG = {("c2", "fp32", 16): [0.7973, 1.0266, 0.9855, 0.7925],
+                    ("c2", "bf16x3", 16): [0.8888, 1.0627, 1.0246, 1.0386],
+                    ("c2s", "fp32", 16): [0.7973, 1.0266, 0.9855, 0.7925],
+                    ("c2s", "bf16x3", 16): [0.8888, 1.0627, 1.0246, 1.0386]}
+NCU_TRAFFIC_SOURCE = {
+    "c2": "ncu DRAM bytes of the same stage in the c2s capture, scaled by algorithmic bytes",
+    "c2s": "ncu capture"}
 ERR_BOUND = 1e-6
 # GB300's dense FP64 rate (nominal; no measured FP64 peak is available)
 FP64_NOMINAL_TFLOPS = 1.25
@@ -99,11 +104,20 @@ def parse():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="bfg", choices=["bfg", "reference"])
-    ap.add_argument("--config", default=os.environ.get("BFG_BENCH_CONFIG", "c2"),
+    ap.add_argument("--config", default=os.environ.get("BFG_BENCH_CONFIG", "c4"),
                     choices=sorted(CONFIGS))
     ap.add_argument("--rhs", type=int, default=0)
-    ap.add_argument("--dense-rows", type=int, default=512)
+    ap.add_argument("--dense-rows", type=int, default=4096,
+                    help="sampled target rows of the dense FP64 check")
+    ap.add_argument("--err-rhs", type=int, default=0,
+                    help="right-hand sides in the error check (0: all)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-c2", action="store_true",
+                    help="skip the 65,536-point workload's block (1 and 16 RHS)")
+    ap.add_argument("--no-cpu-factorization", action="store_true",
+                    help="skip the oracle factorization timings on the host cores")
+    ap.add_argument("--cpu-fac-worker", default="", help=argparse.SUPPRESS)
+    ap.add_argument("--cpu-fac-budget", type=float, default=0.0, help=argparse.SUPPRESS)
     ap.add_argument("--no-gmres", action="store_true",
                     help="skip the multiple-scattering GMRES time-to-1e-8 measurement")
     ap.add_argument("--learned", action="store_true",
@@ -504,17 +518,30 @@ def learned_scattering(B, ctx, train_layouts=6, angles=6, iterates=(0, 20, 60, 1
 
 
 # ---------------------------------------------------------------------------
-# CPU legs (the only place bench.py runs the oracle)
+# CPU legs and the accuracy check (the only places bench.py runs the oracle)
 # ---------------------------------------------------------------------------
-def cpu_port_time(plan_text, data, col_major, X, nthreads, budget_s=20.0):
-    """RHS/s of the reference's apply algorithm (oracle port) on host cores,
-    on a bounded number of RHS."""
+STANDIN_ENTRIES = 1 << 29        # 8 GiB of complex128: the CPU timings' block values
+
+
+def standin_port(plan_text):
+    """The reference's apply algorithm (oracle C port of
+    mat_block_dense/mat_product/mat_block_diag/mat_block_coo Mul) over the
+    plan's structure, with constant stand-in block values (values do not
+    change the cost) in a buffer far larger than the host caches that every
+    block reads in turn."""
     from oracle import bf_oracle as O
-    port = O.ApplyPort.from_plan(plan_text, data, col_major)
+    entries = O.parse_plan_entries(plan_text)
+    data = np.full(min(STANDIN_ENTRIES, entries), 1e-3 + 1e-3j, dtype=np.complex128)
+    return O.ApplyPort.from_plan(plan_text, data, True, wrap=entries > data.size), entries
+
+
+def cpu_port_time(plan_text, X, nthreads, budget_s=20.0):
+    """RHS/s of the reference's apply algorithm on host cores, on the number
+    of right-hand sides that fits the time budget."""
+    port, _ = standin_port(plan_text)
     t0 = time.perf_counter()
     port(X[:, :1], nthreads)
     t1 = time.perf_counter() - t0
-    # grow the sample while it stays within the budget
     Rs = int(max(1, min(X.shape[1], budget_s / 3 / max(t1, 1e-6))))
     Xs = np.ascontiguousarray(X[:, :Rs])
     times = []
@@ -526,10 +553,122 @@ def cpu_port_time(plan_text, data, col_major, X, nthreads, budget_s=20.0):
     return Rs / t, Rs, t
 
 
+class OracleRows(threading.Thread):
+    """Dense FP64 rows of K X from the oracle (glibc Bessel functions, the
+    reference's kernel formulas, helm2.c:93-125, 282-319) on the host cores,
+    in column chunks; runs beside the GPU timing."""
+
+    def __init__(self, k, src_tree, tgt_tree, rows, X):
+        super().__init__(daemon=True)
+        self.args = (k, src_tree, tgt_tree, rows, X)
+        self.result = None
+        self.error = None
+        self.seconds = None
+
+    def run(self):
+        try:
+            from oracle import bf_oracle as O
+            k, src_tree, tgt_tree, rows, X = self.args
+            t0 = time.perf_counter()
+            self.result = O.dense_rows(O.Helm2(k), src_tree, tgt_tree, rows, X)
+            self.seconds = time.perf_counter() - t0
+        except Exception as exc:       # reported with the line
+            self.error = str(exc)[:200]
+
+    def get(self):
+        self.join()
+        return self.result
+
+
+def cpu_factorization_worker(name, budget_s):
+    """One process, thread counts fixed by its environment: the oracle's
+    factorization (the reference's algorithm: glibc kernel fills, scipy
+    zgesvd pseudo-inverses; fac_helm2.c:943-1002, helm2.c:321-365) of the
+    workload -- in full when `budget_s` <= 0, else an estimate from a
+    sample of its blocks drawn with probability proportional to a cost
+    model (Horvitz-Thompson: total ~ mean of time / probability)."""
+    from oracle import bf_oracle as O
+    cfg = CONFIGS[name]
+    src, tgt = workload_inputs(cfg, "reference")
+    t0 = time.perf_counter()
+    fac = O.Factorization(O.Helm2(cfg["k"]), src, tgt, leaf_size=cfg["leaf"], eps=cfg["tol"],
+                          rcut="relative", fill=False)
+    plan_s = time.perf_counter() - t0
+    blocks = fac.blocks()
+    if budget_s <= 0:
+        t0 = time.perf_counter()
+        for b in blocks:
+            fac.fill_block(b)
+        return {"workload": name, "full": True, "seconds": plan_s + time.perf_counter() - t0,
+                "blocks": len(blocks)}
+    # strata of equal modelled cost (blocks sorted by cost); a few blocks
+    # drawn at random from each, timed, and the stratum's total estimated as
+    # its block count times their mean time
+    cost = np.array([22.0 * b.m ** 3 + 16.0 * b.m ** 2 * b.n + 300.0 * (b.m * b.m + b.m * b.n)
+                     if b.kind in ("first", "middle") else 300.0 * b.m * b.n for b in blocks])
+    order = np.argsort(cost)
+    cum = np.cumsum(cost[order]) / cost.sum()
+    G = 10
+    edges = np.searchsorted(cum, np.arange(1, G) / G)
+    strata = [s_ for s_ in np.split(order, edges) if len(s_)]
+    rng = np.random.default_rng(0)
+    times = []
+    for st_ in strata:
+        # at least two blocks per stratum, more while its share of the budget lasts
+        pk = rng.permutation(st_)
+        ts = []
+        t0s = time.perf_counter()
+        for i in pk:
+            if len(ts) >= 2 and time.perf_counter() - t0s > budget_s / len(strata):
+                break
+            b = blocks[int(i)]
+            t0 = time.perf_counter()
+            fac.fill_block(b)
+            ts.append(time.perf_counter() - t0)
+            b.data = None
+        times.append(ts)
+    total, var, n = plan_s, 0.0, 0
+    for st_, ts in zip(strata, times):
+        n += len(ts)
+        total += len(st_) * float(np.mean(ts))
+        if len(ts) > 1:
+            var += (len(st_) ** 2) * float(np.var(ts, ddof=1)) / len(ts)
+    per_stratum = min(len(t_) for t_ in times)
+    return {"workload": name, "full": False, "estimated_seconds": total,
+            "standard_error_s": var ** 0.5, "sampled_blocks": n, "blocks": len(blocks),
+            "sample": "%d strata of equal modelled cost (22 p^3 + 16 p^2 n + 300 kernel "
+                      "evaluations per block), random blocks timed in each (at least %d, more while "
+                      "its tenth of the budget lasts); estimate = "
+                      "sum of stratum size x mean time" % (len(strata), per_stratum)}
+
+
+def cpu_factorization(jobs):
+    """The oracle's factorization timed on the host cores in child processes,
+    with one thread and with all of them (OPENBLAS/OMP thread counts set in
+    the child's environment before numpy loads)."""
+    out = {}
+    ncpu = os.cpu_count() or 1
+    for name, budget in jobs:
+        for threads in (1, ncpu):
+            env = dict(os.environ, OPENBLAS_NUM_THREADS=str(threads), OMP_NUM_THREADS=str(threads))
+            try:
+                r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-fac-worker",
+                                    name, "--cpu-fac-budget", str(budget)],
+                                   env=env, capture_output=True, text=True, timeout=600)
+                res = json.loads(r.stdout.strip().splitlines()[-1])
+            except Exception as exc:
+                res = {"error": str(exc)[:200]}
+            res["threads"] = threads
+            out["%s_%dthread" % (name, threads)] = res
+    return out
+
+
 def run_reference(args):
     """--impl reference: the reference's apply (oracle C port of
     mat_block_dense/mat_product/mat_block_diag/mat_block_coo Mul) on host
-    cores over the same block structure, built by the oracle planner."""
+    cores over the same block structure, built by the oracle planner, with
+    stand-in block values.  Each step applies a bounded number of the
+    workload's RHS."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -543,20 +682,17 @@ def run_reference(args):
                           fill=False)
     plan_s = time.perf_counter() - t0
     text = fac.plan_text()
-    entries = fac.num_entries()
-    # block values do not change the apply's cost; a constant fill stands in
-    # for the factorization (seconds to hours on the CPU)
-    data = np.full(entries, 1e-3 + 1e-3j, dtype=np.complex128)
+    port, entries = standin_port(text)
     rng = O.RefRng(1)
     Xs = rng.complex_randn(cfg["n"] * 1).reshape(cfg["n"], 1)
     Xs = np.ascontiguousarray(np.repeat(Xs, R, axis=1))
     nthreads = os.cpu_count() or 1
-    port = O.ApplyPort.from_plan(text, data, False)
     port(Xs[:, :1], nthreads)
     t0 = time.perf_counter()
     port(Xs[:, :1], nthreads)
     t1 = time.perf_counter() - t0
-    Rs = int(max(1, min(R, 8.0 / max(t1, 1e-6))))
+    # RHS per step: what fits about 5 s (the whole run stays within minutes)
+    Rs = int(max(1, min(R, 5.0 / max(t1, 1e-6))))
     times = []
     for _ in range(max(1, args.warmup)):
         port(Xs[:, :Rs], nthreads)
@@ -566,8 +702,8 @@ def run_reference(args):
         times.append(time.perf_counter() - t0)
     ms = float(np.mean(times)) * 1e3
     value = Rs / (ms / 1e3)
-    sample = ("all %d blocks of the factorization's structure (oracle planner, constant "
-              "block values), %d of %d RHS per step" % (len(fac.blocks()), Rs, R))
+    sample = ("all %d blocks of the factorization's structure (oracle planner; %d entries, "
+              "stand-in values), %d of %d RHS per step" % (len(fac.blocks()), entries, Rs, R))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "RHS/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -582,8 +718,174 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------
+# the single-problem workloads
+# ---------------------------------------------------------------------------
+DTYPES = {"fp64": "complex128", "df64": "double-float (complex128 vectors)",
+          "fp32": "complex64", "bf16x3": "bf16x3 split (complex64 vectors)",
+          "bf16x2": "bf16x2 split (complex64 vectors)"}
+ENTRY_BYTES = {"fp64": 16, "df64": 16, "fp32": 8, "bf16x3": 12, "bf16x2": 8}
+
+
+def hbm_peak():
+    try:
+        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def launch_roofline(fac, X, Y, R, prec):
+    """Per-launch CUDA-event times of one apply (mean of 3) and the
+    algorithmic bytes of each launch (entries x bytes per entry + R x vector
+    bytes x (rows in + rows out)); the dominant launch's achieved GB/s."""
+    per = np.mean(np.array([fac.apply_timed(X.data_ptr(), R, R, Y.data_ptr(), R, prec)
+                            for _ in range(3)], dtype=np.float64), axis=0)
+    info = fac.launch_info()
+    sA = ENTRY_BYTES[prec]
+    sv = 16 if prec in ("fp64", "df64") else 8
+    alg = [float(e * sA + R * sv * (ri + ro)) for e, ri, ro in info]
+    dom = int(np.argmax(per))
+    peak, src = hbm_peak()
+    ach = float(alg[dom] / (per[dom] / 1e3) / 1e9)
+    return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+            "peak_source": src, "kernel": "apply launch %d of %d" % (dom, len(per)),
+            "launch_ms": float(per[dom]), "alg_bytes": alg[dom],
+            "launch_share": [float(v) for v in per / per.sum()],
+            "alg_bytes_per_launch": alg, "launch_ms_all": [float(v) for v in per],
+            "flops_per_s": float(8.0 * info[dom, 0] * R / (per[dom] / 1e3)),
+            "whole_apply_gbs": float(sum(alg) / (per.sum() / 1e3) / 1e9)}
+
+
+def timed(fac, X, Y, R, prec, steps, warmup, stream, dist):
+    """Warm-up applies, one apply captured in a CUDA graph, warm-up replays,
+    then `steps` timed replays with a CUDA event between replays (on the
+    stream the library launches on).  Returns (total ms, median ms, captured)."""
+    import torch
+    for _ in range(warmup):
+        fac.apply_device(X.data_ptr(), R, R, Y.data_ptr(), R, prec)
+    stream.synchronize()
+    graph = None
+    try:
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=stream):
+            fac.apply_device(X.data_ptr(), R, R, Y.data_ptr(), R, prec)
+    except Exception:                  # an uncapturable apply is timed directly
+        graph = None
+        torch.cuda.synchronize()
+
+    def step():
+        if graph is not None:
+            graph.replay()
+        else:
+            fac.apply_device(X.data_ptr(), R, R, Y.data_ptr(), R, prec)
+
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            step()
+    stream.synchronize()
+    barrier(dist)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    with torch.cuda.stream(stream):
+        ev[0].record(stream)
+        for i in range(steps):
+            step()
+            ev[i + 1].record(stream)
+    ev[-1].synchronize()
+    torch.cuda.synchronize()
+    barrier(dist)
+    per = [ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]
+    return ev[0].elapsed_time(ev[-1]), float(np.median(per)), graph is not None
+
+
+def make_fac(B, ctx, cfg, src, tgt):
+    t0 = time.perf_counter()
+    fac = B.FacHelm2.make_multilevel(
+        B.Helm2(cfg["k"]), B.Quadtree(src, leaf_size=cfg["leaf"]),
+        B.Quadtree(tgt, leaf_size=cfg["leaf"]), rank_eps=cfg["tol"], pinv_tol=cfg["tol"],
+        context=ctx)
+    return fac, time.perf_counter() - t0
+
+
+def fac_summary(fac, wall_s):
+    st = fac.stats()
+    return {"wall_s": wall_s, "device_ms": st["factorMs"], "blocks": st["numBlocks"],
+            "bytes_fp64": fac.num_bytes(), "max_rank": st["maxRank"],
+            "jacobi_not_converged": st["jacobiNotConverged"],
+            "sketched_blocks": st["numSketched"], "sketch_ms": st["sketchMs"],
+            "sketch_mean_width": st["sketchMeanWidth"], "sketch_max_width": st["sketchMaxWidth"],
+            "sketch_retries": st["sketchRetries"], "fill_ms": st["fillMs"],
+            "reexp_shared_ms": st["reexpSmemMs"], "reexp_global_ms": st["reexpGlobalMs"],
+            "work": factorization_work(fac.block_table(), st)}
+
+
+def rel_rows(Y, rows, Re, yd):
+    ye = Y[rows][:, :Re].cpu().numpy().astype(np.complex128)
+    return float(np.linalg.norm(ye - yd) / np.linalg.norm(yd))
+
+
+def small_rhs_block(B, fac, ctx, stream, n, R, precs, steps, yd_rows, Xh, dist):
+    """Applies to R (1 or few) right-hand sides: RHS/s, error against the
+    oracle rows, and the dominant launch's HBM roofline per precision."""
+    import torch
+    rows, yd = yd_rows
+    out = {}
+    with torch.cuda.stream(stream):
+        X64 = torch.from_numpy(np.ascontiguousarray(Xh[:, :R])).to("cuda")
+        X32 = X64.to(torch.complex64)
+        Y64 = torch.empty((n, R), dtype=torch.complex128, device="cuda")
+        Y32 = torch.empty((n, R), dtype=torch.complex64, device="cuda")
+    stream.synchronize()
+    for p in precs:
+        X, Y = (X64, Y64) if p in ("fp64", "df64") else (X32, Y32)
+        fac.apply_device(X.data_ptr(), R, R, Y.data_ptr(), R, p)
+        stream.synchronize()
+        err = rel_rows(Y, rows, R, yd[:, :R]) if yd is not None else None
+        tot, med, _ = timed(fac, X, Y, R, p, steps, 3, stream, dist)
+        roof = launch_roofline(fac, X, Y, R, p)
+        out[p] = {"rhs_per_s": R * steps / (tot / 1e3), "ms_per_apply": tot / steps,
+                  "rel_err": err, "dominant_launch_gbs": roof["achieved"],
+                  "dominant_launch_frac_of_measured_hbm": roof["frac"],
+                  "whole_apply_gbs": roof["whole_apply_gbs"],
+                  "whole_apply_tflops": float(fac.stats()["flopsPerRhs"] * R / (tot / steps / 1e3) / 1e12)}
+    return out
+
+
+def secondary_c2(B, ctx, stream, args, dist):
+    """The 65,536-point ellipse workload (k = 512, tolerance 1e-10) in the
+    same run: factorization time, 1- and 16-RHS applies with errors against
+    oracle rows and HBM rates."""
+    cfg = CONFIGS["c2"]
+    n = cfg["n"]
+    src, tgt = workload_inputs(cfg, "bfg")
+    fac, wall = make_fac(B, ctx, cfg, src, tgt)
+    sp, tp = fac.perms()
+    Xh = B.Rng(99).complex_randn(n * 16).reshape(n, 16)
+    rows = np.unique(np.linspace(0, n - 1, min(args.dense_rows, n)).astype(np.int64))
+    orows = OracleRows(cfg["k"], src[sp], tgt[tp], rows, Xh)
+    orows.start()
+    yd = orows.get()
+    res = {"workload": "helmholtz2d_butterfly_apply_c2", "n": n, "k": cfg["k"],
+           "tolerance": cfg["tol"], "factorization": fac_summary(fac, wall),
+           "err_rows": int(len(rows)), "oracle_rows_s": orows.seconds}
+    if yd is None:
+        res["error"] = orows.error
+        yd_rows = (rows, None)
+    else:
+        yd_rows = (rows, yd)
+    res["rhs1"] = small_rhs_block(B, fac, ctx, stream, n, 1, ("fp64", "df64", "fp32", "bf16x3"),
+                                  20, yd_rows, Xh, dist)
+    res["rhs16"] = small_rhs_block(B, fac, ctx, stream, n, 16,
+                                   ("fp64", "df64", "fp32", "bf16x3", "bf16x2"), 10, yd_rows, Xh,
+                                   dist)
+    fac.close()
+    return res
+
+
 def main():
     args = parse()
+    if args.cpu_fac_worker:
+        print(json.dumps(cpu_factorization_worker(args.cpu_fac_worker, args.cpu_fac_budget)))
+        return
     if CONFIGS[args.config].get("batched"):
         if args.impl == "reference":
             if int(os.environ.get("RANK", "0")) == 0:
@@ -607,109 +909,95 @@ def main():
     n = cfg["n"]
     ctx = B.Context(local)
     src, tgt = workload_inputs(cfg, "bfg")
-
-    t0 = time.perf_counter()
-    fac = B.FacHelm2.make_multilevel(
-        B.Helm2(cfg["k"]), B.Quadtree(src, leaf_size=cfg["leaf"]),
-        B.Quadtree(tgt, leaf_size=cfg["leaf"]), rank_eps=cfg["tol"], pinv_tol=cfg["tol"],
-        context=ctx)
-    fac_wall_s = time.perf_counter() - t0
-    st = fac.stats()
+    fac, fac_wall_s = make_fac(B, ctx, cfg, src, tgt)
+    sp, tp = fac.perms()
 
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
     rng = B.Rng(1234 + rank)
-    Xh = rng.complex_randn(n * R).reshape(n, R)
+    Xh = rng.complex_randn(n * R).reshape(n, R)           # tree order, as A X takes it
+    # accuracy: dense FP64 rows from the oracle on the host cores, computed
+    # while the GPU is timed; the library's own GPU evaluator cross-checks it
+    Re = min(R, args.err_rhs) if args.err_rhs > 0 else R
+    rows = np.unique(np.linspace(0, n - 1, min(args.dense_rows, n)).astype(np.int64))
+    orows = None
+    if rank == 0:
+        orows = OracleRows(cfg["k"], src[sp], tgt[tp], rows, np.ascontiguousarray(Xh[:, :Re]))
+        orows.start()
     with torch.cuda.stream(stream):
         X64 = torch.from_numpy(Xh).to("cuda")
         X32 = X64.to(torch.complex64)
         Y64 = torch.empty((n, R), dtype=torch.complex128, device="cuda")
         Y32 = torch.empty((n, R), dtype=torch.complex64, device="cuda")
-    stream.synchronize()
-
-    # accuracy: dense FP64 rows on the GPU (the product's FP64 kernel
-    # evaluator; validated against the CPU oracle in the tests)
-    Re = min(R, 16)
-    rows = np.unique(np.linspace(0, n - 1, min(args.dense_rows, n)).astype(np.int64))
-    with torch.cuda.stream(stream):
-        Xe = X64[:, :Re].contiguous()
-        yd = fac.dense_rows(rows, Xe, Re)
-    stream.synchronize()
-    yd = yd.cpu().numpy()
-
-    with torch.cuda.stream(stream):
         Y16 = torch.empty((n, R), dtype=torch.complex64, device="cuda")
+        Ydf = torch.empty_like(Y64)
     stream.synchronize()
-    # bf16x3 / bf16x2: tensor-core products of split-BF16 planes, complex64 vectors
     # the tensor-core schedules: per stage the fastest of several CTA dealings
     # (bfgFacAutotune), before anything is timed
     tuned = {}
     for p in ("bf16x3", "bf16x2"):
         t = fac.autotune(p, R)
         tuned[p] = {"default_ms": [float(v) for v in t[:, 0]], "tuned_ms": [float(v) for v in t[:, 1]]}
-    # df64: FP64-accurate double-float arithmetic, complex128 vectors
-    with torch.cuda.stream(stream):
-        Ydf = torch.empty_like(Y64)
-    stream.synchronize()
     precs = {"fp64": (X64, Y64), "df64": (X64, Ydf), "fp32": (X32, Y32), "bf16x3": (X32, Y16),
              "bf16x2": (X32, Y16)}
-    errs = {}
+    outs = {}
+    apply_ms = {}
     for p, (X, Y) in precs.items():
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
         fac.apply_device(X.data_ptr(), R, R, Y.data_ptr(), R, p)
         stream.synchronize()
-        ye = Y[rows][:, :Re].cpu().numpy().astype(np.complex128)
-        errs[p] = float(np.linalg.norm(ye - yd) / np.linalg.norm(yd))
+        apply_ms[p] = (time.perf_counter() - t0) * 1e3
+        outs[p] = Y[rows][:, :Re].cpu().numpy().astype(np.complex128)
+    # GPU evaluator rows (cross-check of the oracle rows)
+    Rg = min(Re, 16)
+    with torch.cuda.stream(stream):
+        yg = fac.dense_rows(rows, X64[:, :Rg].contiguous(), Rg)
+    stream.synchronize()
+    yg = yg.cpu().numpy()
 
+    # K timed steps for the precisions whose apply takes under a second, 3
+    # for the slower FP64 forms (the ratio's denominator), W >= 3 warm-ups
     clocks = ClockSampler(local)
     clocks.start()
-    tm = {p: graph_timed(fac, precs[p][0], precs[p][1], R, p, args, stream, dist) for p in precs}
+    steps_p = {p: (args.steps if apply_ms[p] < 1000 else min(args.steps, 3)) for p in precs}
+    warm_p = {p: (max(3, args.warmup) if apply_ms[p] < 1000 else 1) for p in precs}
+    tm = {p: timed(fac, precs[p][0], precs[p][1], R, p, steps_p[p], warm_p[p], stream, dist)
+          for p in precs}
     clk = clocks.stop()
     total_ms = {p: max_over_ranks(v[0], dist) for p, v in tm.items()}
     median_ms = {p: v[1] for p, v in tm.items()}
     captured = all(v[2] for v in tm.values())
-    rhs_s = {p: world * R * args.steps / (total_ms[p] / 1e3) for p in precs}
+    rhs_s = {p: world * R * steps_p[p] / (total_ms[p] / 1e3) for p in precs}
+
+    yd = orows.get() if orows is not None else None
+    err_src = "oracle"
+    if yd is None:                     # fall back to the GPU evaluator, and say so
+        yd, err_src = yg, "gpu evaluator (oracle rows failed: %s)" % (orows.error if orows else "")
+        Re = Rg
+    errs = {p: float(np.linalg.norm(outs[p][:, :Re] - yd[:, :Re]) / np.linalg.norm(yd[:, :Re]))
+            for p in precs}
+    gpu_rows_vs_oracle = (float(np.linalg.norm(yg - yd[:, :Rg]) / np.linalg.norm(yd[:, :Rg]))
+                          if err_src == "oracle" else None)
     ok = [p for p in precs if errs[p] <= ERR_BOUND]
     head = max(ok, key=lambda p: rhs_s[p]) if ok else "fp64"
 
-    # roofline of the dominant launch of the headline precision
     X, Y = precs[head]
-    per = []
-    for _ in range(3):
-        per.append(fac.apply_timed(X.data_ptr(), R, R, Y.data_ptr(), R, head))
-    per = np.mean(np.array(per, dtype=np.float64), axis=0)
-    info = fac.launch_info()
-    dom = int(np.argmax(per))
-    sA = {"fp64": 16, "df64": 16, "fp32": 8, "bf16x3": 12, "bf16x2": 8}[head]
-    sv = 16 if head in ("fp64", "df64") else 8
-    alg_all = [float(e * sA + R * sv * (ri + ro)) for e, ri, ro in info]
-    alg_bytes = alg_all[dom]
-    launch_share = [float(v) for v in per / per.sum()]
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-        peak, peak_src = float(peaks["hbm_gbs"]), "measured"
-    except (OSError, KeyError, ValueError):
-        peak, peak_src = 6800.0, "fallback"
-    achieved = float(alg_bytes / (per[dom] / 1e3) / 1e9)
-    ratios = NCU_DRAM_PER_ALG.get((head, R, len(per)))
-    traffic, traffic_src = None, None
-    if ratios is not None and args.config in ("c2", "c2s") and dom < len(ratios):
-        traffic = float(ratios[dom] * alg_bytes)
-        traffic_src = ("ncu DRAM bytes of the same stage in the c2s capture, scaled by "
-                       "algorithmic bytes" if args.config == "c2" else "ncu capture")
-    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
-            "peak_source": peak_src,
-            "kernel": "apply launch %d of %d" % (dom, len(per)),
-            "launch_ms": float(per[dom]), "alg_bytes": alg_bytes,
-            "launch_share": launch_share, "alg_bytes_per_launch": alg_all,
-            "flops_per_s": float(8.0 * info[dom, 0] * R / (per[dom] / 1e3))}
+    roof = launch_roofline(fac, X, Y, R, head)
+    ratios = NCU_DRAM_PER_ALG.get((args.config, head, R))
+    roof["traffic"] = None
+    if ratios is not None:
+        dom = int(roof["kernel"].split()[2])
+        if dom < len(ratios):
+            roof["traffic"] = float(ratios[dom] * roof["alg_bytes"])
+            roof["traffic_source"] = NCU_TRAFFIC_SOURCE[args.config]
 
     # end to end through the C ABI with pinned host complex128 operands, two
     # input/output pairs used in turn: the pipelined call
     # (bfgFacApplyHostAsync: one step's upload and download overlap another
     # step's compute) with one wait at the end, and the synchronous call
     # (bfgFacApplyHost) timed beside it
+    e2e_steps = steps_p[head]
     Xp = [torch.from_numpy(Xh).pin_memory() for _ in range(2)]
     Yp = [torch.empty((n, R), dtype=torch.complex128).pin_memory() for _ in range(2)]
     lib = B.lib()
@@ -730,24 +1018,50 @@ def main():
         host_steps(2, pipelined)
         barrier(dist)
         t0 = time.perf_counter()
-        host_steps(args.steps, pipelined)
+        host_steps(e2e_steps, pipelined)
         e2e_t[pipelined] = max_over_ranks(time.perf_counter() - t0, dist)
-    e2e = {"value": world * R * args.steps / e2e_t[True], "unit": "RHS/s",
+    e2e = {"value": world * R * e2e_steps / e2e_t[True], "unit": "RHS/s",
            "h2d_bytes_per_step": n * R * 16, "d2h_bytes_per_step": n * R * 16,
            "precision": head, "call": "bfgFacApplyHostAsync (pipelined), one wait",
-           "synchronous_call_value": world * R * args.steps / e2e_t[False]}
+           "steps": e2e_steps,
+           "synchronous_call_value": world * R * e2e_steps / e2e_t[False]}
+    del Xp, Yp
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        tab, ent = fac.blocks()
-        nthreads = os.cpu_count() or 1
-        v, Rs, t = cpu_port_time(fac.describe(), ent, True, Xh, nthreads)
-        cpu = {"value": v, "unit": "RHS/s", "cores": nthreads, "kind": "port",
-               "sample": "full operator (%d blocks, this factorization), %d RHS, median of 3"
-                         % (len(tab), Rs)}
+    # one right-hand side: the HBM-bound single-vector apply
+    rhs1 = small_rhs_block(B, fac, ctx, stream, n, 1, ("fp64", "df64", "fp32", "bf16x3"), 10,
+                           (rows, yd), Xh, dist) if rank == 0 else None
+    fac_info = fac_summary(fac, fac_wall_s)
+    plan_text = fac.describe()
+    launches = len(fac.launch_info()) * steps_p[head]
+    fac.close()
+    del precs, X64, X32, Y64, Y32, Y16, Ydf, X, Y
+    torch.cuda.empty_cache()
 
     if rank != 0:
         return
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        v, Rs, t = cpu_port_time(plan_text, Xh, nthreads)
+        cpu = {"value": v, "unit": "RHS/s", "cores": nthreads, "kind": "port",
+               "sample": "the reference's apply algorithm (oracle C port) over this "
+                         "factorization's structure with stand-in values, %d of %d RHS, "
+                         "median of 3" % (Rs, R)}
+    c2 = None
+    if world == 1 and not args.no_c2 and args.config != "c2":
+        try:
+            c2 = secondary_c2(B, ctx, stream, args, dist)
+        except Exception as exc:
+            c2 = {"error": str(exc)[:200]}
+    cpu_fac = None
+    if world == 1 and not args.no_cpu_factorization:
+        cpu_fac = cpu_factorization([("c1", 0), ("c2", 10.0)])
+        try:
+            f1, w1 = make_fac(B, ctx, CONFIGS["c1"], *workload_inputs(CONFIGS["c1"], "bfg"))
+            cpu_fac["gpu_c1"] = {"wall_s": w1, "device_ms": f1.stats()["factorMs"]}
+            f1.close()
+        except Exception as exc:
+            cpu_fac["gpu_c1"] = {"error": str(exc)[:200]}
     gm = None
     if world == 1 and not args.no_gmres:
         try:
@@ -759,28 +1073,22 @@ def main():
                 gm["learned"] = learned_scattering(B, ctx)
             except Exception as exc:
                 gm["learned"] = {"error": str(exc)[:200]}
-    launches = len(fac.launch_info()) * args.steps
     line = {"metric": METRIC, "value": rhs_s[head], "unit": "RHS/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": total_ms[head] / args.steps, "median_ms_per_step": median_ms[head],
+            "ms_per_step": total_ms[head] / steps_p[head], "median_ms_per_step": median_ms[head],
             "graph_captured": captured, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None,
-            "dtype": {"fp64": "complex128", "df64": "double-float (complex128 vectors)",
-                      "fp32": "complex64",
-                      "bf16x3": "bf16x3 split (complex64 vectors)",
-                      "bf16x2": "bf16x2 split (complex64 vectors)"}[head],
+            "scaling": "weak", "vs_baseline": None, "dtype": DTYPES[head],
             "data": "synthetic", "config": config_json(args.config, cfg, R),
             "precision": head, "rel_err": errs[head], "rel_err_all": errs,
-            "rhs_per_s_all": rhs_s, "err_bound": ERR_BOUND,
-            "err_rows": int(len(rows)), "err_rhs": Re,
+            "rhs_per_s_all": rhs_s, "steps_per_precision": steps_p, "err_bound": ERR_BOUND,
+            "err_rows": int(len(rows)), "err_rhs": Re, "err_reference": err_src,
+            "oracle_rows_s": orows.seconds if orows else None,
+            "gpu_rows_vs_oracle": gpu_rows_vs_oracle,
             "fp64_speedup": rhs_s[head] / rhs_s["fp64"],
-            "factorization": {"wall_s": fac_wall_s, "device_ms": st["factorMs"],
-                              "blocks": st["numBlocks"], "bytes_fp64": fac.num_bytes(),
-                              "max_rank": st["maxRank"],
-                              "jacobi_not_converged": st["jacobiNotConverged"],
-                              "work": factorization_work(fac.block_table(), st)},
+            "factorization": fac_info, "rhs1": rhs1,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-            "gpu_launches": launches, "gmres": gm, "autotune": tuned}
+            "gpu_launches": launches, "gmres": gm, "autotune": tuned,
+            "cpu_factorization": cpu_fac, "c2": c2}
     print(json.dumps(line))
 
 

@@ -74,7 +74,8 @@ class _FacStatsC(ctypes.Structure):
             "factorMs", "flopsPerRhs", "fillMs", "reexpSmemMs", "reexpGlobalMs")] + [
         (n, ctypes.c_int64) for n in (
             "numSketched", "sketchRetries", "sketchFallbacks", "sketchMaxWidth")] + [
-        (n, ctypes.c_double) for n in ("sketchMs", "sketchMeanWidth")]
+        (n, ctypes.c_double) for n in ("sketchMs", "sketchMeanWidth")] + [
+        ("applyBufferBytes", ctypes.c_int64)]
 
 
 class _RngC(ctypes.Structure):

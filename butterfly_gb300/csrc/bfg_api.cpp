@@ -1240,6 +1240,7 @@ bfgStatus bfgFacNumBytes(bfgFac f, int64_t *bytes) {
 bfgStatus bfgFacGetStats(bfgFac f, bfgFacStats *st) {
   if (!f || !st) return BFG_ERROR_INVALID_ARGUMENTS;
   *st = f->stats;
+  st->applyBufferBytes = (int64_t)(f->ws.bytes + f->xbuf.bytes);
   return BFG_OK;
 }
 

@@ -25,6 +25,7 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <climits>
 #include <mutex>
 
 #include "../../include/bfg.h"
@@ -58,13 +59,17 @@ extern "C" bfgStatus bfgFacApplyNoAlloc(bfgFac fac, void const *X, int64_t ldx, 
                             "no-alloc apply: bad operand pointers or shapes");
   if (flags & ~BFG_APPLY_ORIGINAL_ORDER)
     return bfg::noAllocFail(fac, BFG_ERROR_INVALID_ARGUMENTS, "no-alloc apply: unknown flags");
-  int64_t const need = bfg::noAllocWorkspaceEntries(fac, numRhs, flags);
+  // entries per right-hand side first, so that a huge numRhs is refused
+  // before any product can overflow
+  int64_t const perRhs = bfg::noAllocWorkspaceEntries(fac, 1, flags);
+  bool const tooMany = perRhs > 0 && numRhs > (int64_t)kNoAllocScratchEntries / perRhs;
+  int64_t const need = tooMany ? INT64_MAX : perRhs * numRhs;
   if (need > (int64_t)kNoAllocScratchEntries) {
     char msg[256];
     std::snprintf(msg, sizeof msg,
-                  "no-alloc apply: needs %lld bytes of workspace, the static limit is %zu bytes "
+                  "no-alloc apply: needs %lld bytes of workspace (-1: more than 2^63), the static limit is %zu bytes "
                   "(%lld right-hand sides too many; use bfgFacApply)",
-                  (long long)(need * (int64_t)sizeof(double2)), kNoAllocScratchBytes,
+                  (long long)(tooMany ? -1 : need * (int64_t)sizeof(double2)), kNoAllocScratchBytes,
                   (long long)numRhs);
     return bfg::noAllocFail(fac, BFG_ERROR_OUT_OF_RANGE, msg);
   }

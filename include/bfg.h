@@ -130,6 +130,9 @@ typedef struct bfgFacStats {
   int64_t sketchMaxWidth;     /* widest accepted sketch */
   double sketchMs;            /* device time of the randomized path */
   double sketchMeanWidth;     /* mean accepted sketch width */
+  int64_t applyBufferBytes;   /* device bytes the allocating applies have
+                                 allocated so far (workspace and gather
+                                 buffers; bfgFacApplyNoAlloc adds none) */
 } bfgFacStats;
 
 /* Contexts: one CUDA device and one stream; calls on a context are

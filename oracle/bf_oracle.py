@@ -675,11 +675,13 @@ def kernel_matrix(helm: Helm2, src, tgt, src_normals=None, tgt_normals=None):
 
 
 def lstsq_pinv(A: np.ndarray, B: np.ndarray, rcut: str = "reference",
-               tol: float = None) -> np.ndarray:
+               tol: float = None, return_terms: bool = False):
     """bfMatDenseComplexDenseComplexLstSq (mat_dense_complex.c:1768-1849):
     X = V_k S_k^-1 U_k^H B with k = #{sigma_i >= max(m,n) eps sigma_0 + eps}.
     ``rcut="relative"`` keeps sigma_i >= tol * sigma_0 instead (the
-    truncation rule of bfTruncSpecGetNumTerms, linalg.c:26-36)."""
+    truncation rule of bfTruncSpecGetNumTerms, linalg.c:26-36).
+    ``return_terms``: also the number of kept terms and the singular
+    values."""
     import scipy.linalg
     m, n = A.shape
     U, S, VH = scipy.linalg.svd(A, full_matrices=False, lapack_driver="gesvd")
@@ -692,7 +694,8 @@ def lstsq_pinv(A: np.ndarray, B: np.ndarray, rcut: str = "reference",
         k += 1
     tmp1 = U[:, :k].conj().T @ B
     tmp2 = tmp1 / S[:k, None]
-    return VH[:k, :].conj().T @ tmp2
+    X = VH[:k, :].conj().T @ tmp2
+    return (X, k, S) if return_terms else X
 
 
 def sketch_width(k: float, ceq, cchk, m: int, scale: float = 1.15, pad: int = 48) -> int:
@@ -887,16 +890,26 @@ class ApplyPort:
             self.nrows = len(fac.tgt_perm)
 
     @classmethod
-    def from_plan(cls, text: str, data: np.ndarray, col_major: bool):
+    def from_plan(cls, text: str, data: np.ndarray, col_major: bool, wrap: bool = False):
         """Port over the structure of a plan text (oracle_dump grammar) with
         the blocks stored back to back in plan order in ``data`` --
-        row-major, or column-major as in the GPU arena."""
+        row-major, or column-major as in the GPU arena.  ``wrap``: ``data``
+        is a stand-in shorter than the plan (timing only: values do not
+        change the cost); block offsets wrap around it, every block reading
+        its own contiguous m*n entries of it.  It must hold the largest
+        block; far larger than the host caches, it streams from memory as
+        the real factors would."""
         root = parse_plan(text)
         off = [0]
 
         def take(m, n):
             o = off[0]
             off[0] += m * n
+            if wrap:
+                span = data.size - m * n + 1
+                if span <= 0:
+                    raise ValueError("stand-in data shorter than a block")
+                o %= span
             return o
 
         terms, factors, fblocks = [], [], []
@@ -923,7 +936,7 @@ class ApplyPort:
                 terms.append((1, group, r0, c0, m, n, ff, len(nd.factors), 0))
 
         rec(root, 0, 0, None)
-        if off[0] > data.size:
+        if off[0] > data.size and not wrap:
             raise ValueError("block data shorter than the plan")
         p = cls()
         term_dt = np.dtype([("kind", "<i4"), ("group", "<i4"), ("tgtRow", "<i8"),
@@ -956,6 +969,22 @@ class ApplyPort:
         if rc != 0:
             raise MemoryError("apply port failed")
         return Y
+
+
+def parse_plan_entries(text: str) -> int:
+    """Complex entries over all stored blocks of a plan text: the "B" lines
+    of block-diagonal (m n) and block-COO (i j m n) factors and the dense
+    blocks ("DC m n")."""
+    total = 0
+    for line in text.splitlines():
+        t = line.split()
+        if not t:
+            continue
+        if t[0] == "B":
+            total += int(t[-2]) * int(t[-1])
+        elif t[0] == "DC":
+            total += int(t[1]) * int(t[2])
+    return total
 
 
 def parse_plan(text: str):

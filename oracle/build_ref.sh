@@ -62,4 +62,7 @@ gcc -std=gnu11 -O2 -DBF_DOUBLE -DBF_LINUX -I"$REF/include" -I"$HERE/ref_shim" \
     "$HERE/ref_dump.c" -o "$OUT/ref_dump" -L"$OUT" -lbf_ref "$OPENBLAS" -lm \
     -Wl,-rpath,"$OUT" -Wl,-rpath,"$(dirname "$OPENBLAS")"
 
+# where the reference lies (its headers compile tests/integration's adapter)
+echo "$REF" > "$OUT/reference_root.txt"
+echo "$OPENBLAS" > "$OUT/openblas_path.txt"
 echo "build_ref: built $OUT/libbf_ref.so and $OUT/ref_dump"

@@ -99,6 +99,12 @@ int oracle_kernel_matrix(int layerPot, double k, double alphaRe, double alphaIm,
                          double const *snx, double const *sny, int64_t n,
                          cplx *out) {
   cplx const alpha = alphaRe + I * alphaIm, beta = betaRe + I * betaIm;
+  if (layerPot != LP_SINGLE && layerPot != LP_PV_DOUBLE &&
+      layerPot != LP_PV_NORMAL_DERIV_SINGLE && layerPot != LP_COMBINED_FIELD)
+    return -1;
+  /* rows are independent: the host cores split them (same values whatever
+   * the thread count) */
+#pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < m; ++i) {
     for (int64_t j = 0; j < n; ++j) {
       double r = hypot(sx[j] - tx[i], sy[j] - ty[i]);
@@ -125,8 +131,6 @@ int oracle_kernel_matrix(int layerPot, double k, double alphaRe, double alphaIm,
           cplx D = scale * dot;
           z = alpha * S + beta * D;
         }
-      } else {
-        return -1;
       }
       out[i * n + j] = z;
     }

@@ -42,3 +42,38 @@ def test_batched_problems_match_single_factorizations():
         assert np.array_equal(bsp[s0:s1] - s0, sp)
         assert np.array_equal(btp[t0:t1] - t0, tp)
         assert ("PROBLEM %d\n" % p + single.describe()) in text
+
+
+def test_batched_problems_against_the_oracle():
+    """The batched workload's knobs (leaf 64, tolerance 1e-8 for the rank
+    estimate and the relative pseudo-inverse cut) on four uneven problems:
+    each problem's rows of the one batched apply against the oracle's own
+    factorization of that problem (the reference's algorithm with scipy's
+    zgesvd, fac_helm2.c:943-1002) and against dense FP64 rows."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from oracle import bf_oracle as O
+    ctx = B.default_context(0)
+    sizes = [1024, 1733, 2980, 4096]
+    problems = [(B.uniform_square_points(n, 300 + p), B.curve_points("circle", n))
+                for p, n in enumerate(sizes)]
+    ks = [n / 30.0 for n in sizes]
+    tol = 1e-8
+    fac = B.make_batched(B.Helm2(1.0), problems, ks, leaf_size=64, rank_eps=tol, pinv_tol=tol,
+                         context=ctx)
+    R = 2
+    X = B.Rng(9).complex_randn(sum(sizes) * R).reshape(-1, R)
+    Y = fac.apply(X)
+    bsp, btp = fac.perms()
+    for p, ((src, tgt), k) in enumerate(zip(problems, ks)):
+        s0, s1 = fac.src_offsets[p], fac.src_offsets[p + 1]
+        t0, t1 = fac.tgt_offsets[p], fac.tgt_offsets[p + 1]
+        of = O.Factorization(O.Helm2(k), src, tgt, leaf_size=64, eps=tol, rcut="relative")
+        assert np.array_equal(bsp[s0:s1] - s0, of.src_perm)
+        assert np.array_equal(btp[t0:t1] - t0, of.tgt_perm)
+        yo = of.apply(X[s0:s1])
+        assert rel_err(Y[t0:t1], yo) < 1e-6
+        rows = np.arange(0, t1 - t0, 7)
+        yd = O.dense_rows(O.Helm2(k), of.src_tree_pts, of.tgt_tree_pts, rows, X[s0:s1])
+        assert rel_err(Y[t0:t1][rows], yd) < 1e-6
+        assert rel_err(yo[rows], yd) < 1e-6

@@ -192,6 +192,24 @@ def test_dense_rows_on_gpu_match_oracle(ctx):
     assert rel_err(yd, g["y_dense"][:16]) < 1e-12
 
 
+def test_dense_rows_on_gpu_match_oracle_at_higher_wavenumber(ctx):
+    """The GPU's dense-row evaluator (bfgFacDenseRows), which cross-checks
+    the benchmark's oracle rows, against the oracle's rows (glibc Bessel
+    functions, helm2.c:282-319) on 512 rows x 4 RHS at k = 256."""
+    n, k = 16384, 256.0
+    src = O.uniform_square_points(n, 0)
+    tgt = O.curve_points("ellipse", n)
+    fac = B.FacHelm2.make_multilevel(B.Helm2(k), B.Quadtree(src, leaf_size=64),
+                                     B.Quadtree(tgt, leaf_size=64), rank_eps=1e-10,
+                                     pinv_tol=1e-10, context=ctx)
+    sp, tp = fac.perms()
+    X = O.RefRng(4).complex_randn(n * 4).reshape(n, 4)
+    rows = np.linspace(0, n - 1, 512).astype(np.int64)
+    yg = fac.dense_rows(rows, torch.from_numpy(X).cuda(), 4).cpu().numpy()
+    yo = O.dense_rows(O.Helm2(k), src[sp], tgt[tp], rows, X)
+    assert rel_err(yg, yo) < 1e-12
+
+
 def test_tolerance_and_leaf_options_against_dense(ctx):
     """The workloads' knobs (leaf size, rank tolerance, relative pseudo-
     inverse cut) trade accuracy for size; the result is checked against the

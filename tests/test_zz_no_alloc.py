@@ -39,6 +39,17 @@ def test_no_alloc_apply_matches_apply_on_consecutive_calls():
                                      B.Quadtree(g["tgt"]), context=ctx)
     n = fac.shape[1]
     R = 3
+    # on a fresh factorization the no-alloc calls (tree and original order)
+    # leave the factorization's own workspace and gather buffers unallocated
+    X0 = torch.from_numpy(B.Rng(10).complex_randn(n * R).reshape(n, R)).cuda()
+    Y0 = torch.empty_like(X0)
+    ctx.check(_no_alloc(fac, X0, Y0, R), "first no-alloc call")
+    ctx.check(_no_alloc(fac, X0, Y0, R, flags=B.APPLY_ORIGINAL_ORDER), "original order")
+    torch.cuda.synchronize()
+    assert fac.stats()["applyBufferBytes"] == 0
+    Y0_ref = fac.apply(X0, original_order=True)
+    assert fac.stats()["applyBufferBytes"] > 0                # the allocating path did allocate
+    assert rel_err(Y0.cpu().numpy(), Y0_ref.cpu().numpy()) < 1e-13
     for call, seed in enumerate((11, 12)):
         X = torch.from_numpy(B.Rng(seed).complex_randn(n * R).reshape(n, R)).cuda()
         Y_ref = fac.apply(X)                                  # allocating entry point
@@ -65,3 +76,11 @@ def test_no_alloc_apply_matches_apply_on_consecutive_calls():
     st = _no_alloc(fac, Xb, Yb, Rbig)
     assert st == 5                                            # BFG_ERROR_OUT_OF_RANGE
     assert "static limit" in B.lib().bfgGetErrorString(ctx.handle).decode()
+    # a right-hand-side count whose workspace size would overflow 64 bits is
+    # refused the same way, before any device work (the operands are never read)
+    Rhuge = 1 << 62
+    fn = B.lib().bfgFacApplyNoAlloc
+    for flags in (0, B.APPLY_ORIGINAL_ORDER):
+        st = fn(fac.handle, Xb.data_ptr(), Rhuge, Rhuge, Yb.data_ptr(), Rhuge, flags)
+        assert st == 5
+        assert "static limit" in B.lib().bfgGetErrorString(ctx.handle).decode()
