@@ -726,17 +726,34 @@ DTYPES = {"fp64": "complex128", "df64": "double-float (complex128 vectors)",
 ENTRY_BYTES = {"fp64": 16, "df64": 16, "fp32": 8, "bf16x3": 12, "bf16x2": 8}
 
 
-def hbm_peak():
+def measured_peaks():
+    """HBM GB/s and dense bf16 TFLOP/s (burst) measured on the GB300s,
+    else the fallback figures."""
     try:
-        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]), "measured"
+        pk = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(pk["hbm_gbs"]), float(pk["bf16_tflops"]), "measured"
     except (OSError, KeyError, ValueError):
-        return 6800.0, "fallback"
+        return 6800.0, 1900.0, "fallback"
+
+
+def hbm_peak():
+    hbm, _, src = measured_peaks()
+    return hbm, src
+
+
+# tensor-core products per stored entry and right-hand side: planes of A
+# times planes of x kept (bf16x3: hh hm hl mh mm lh; bf16x2: hh hl lh), each
+# 8 real flops per complex multiply-add
+TC_PRODUCTS = {"bf16x3": 6, "bf16x2": 3}
 
 
 def launch_roofline(fac, X, Y, R, prec):
     """Per-launch CUDA-event times of one apply (mean of 3) and the
     algorithmic bytes of each launch (entries x bytes per entry + R x vector
-    bytes x (rows in + rows out)); the dominant launch's achieved GB/s."""
+    bytes x (rows in + rows out)); the dominant launch against HBM and, for
+    the tensor-core precisions, against the bf16 tensor peak (algorithmic
+    flops, 8 per complex multiply-add, and the executed plane products).  The
+    roof the dominant launch is closer to is the reported bound."""
     per = np.mean(np.array([fac.apply_timed(X.data_ptr(), R, R, Y.data_ptr(), R, prec)
                             for _ in range(3)], dtype=np.float64), axis=0)
     info = fac.launch_info()
@@ -744,15 +761,28 @@ def launch_roofline(fac, X, Y, R, prec):
     sv = 16 if prec in ("fp64", "df64") else 8
     alg = [float(e * sA + R * sv * (ri + ro)) for e, ri, ro in info]
     dom = int(np.argmax(per))
-    peak, src = hbm_peak()
-    ach = float(alg[dom] / (per[dom] / 1e3) / 1e9)
-    return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-            "peak_source": src, "kernel": "apply launch %d of %d" % (dom, len(per)),
-            "launch_ms": float(per[dom]), "alg_bytes": alg[dom],
-            "launch_share": [float(v) for v in per / per.sum()],
-            "alg_bytes_per_launch": alg, "launch_ms_all": [float(v) for v in per],
-            "flops_per_s": float(8.0 * info[dom, 0] * R / (per[dom] / 1e3)),
-            "whole_apply_gbs": float(sum(alg) / (per.sum() / 1e3) / 1e9)}
+    hbm, bf16, src = measured_peaks()
+    t = per[dom] / 1e3
+    ach = float(alg[dom] / t / 1e9)
+    alg_tf = float(8.0 * info[dom, 0] * R / t / 1e12)
+    out = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+           "peak_source": src, "kernel": "apply launch %d of %d" % (dom, len(per)),
+           "launch_ms": float(per[dom]), "alg_bytes": alg[dom],
+           "launch_share": [float(v) for v in per / per.sum()],
+           "alg_bytes_per_launch": alg, "launch_ms_all": [float(v) for v in per],
+           "flops_per_s": alg_tf * 1e12,
+           "whole_apply_gbs": float(sum(alg) / (per.sum() / 1e3) / 1e9),
+           "hbm": {"achieved_gbs": ach, "peak_gbs": hbm, "frac": ach / hbm}}
+    if prec in TC_PRODUCTS:
+        exe = alg_tf * TC_PRODUCTS[prec]
+        out["tensor"] = {"achieved_alg_tflops": alg_tf, "executed_tflops_min": exe,
+                         "peak_tflops": bf16, "frac_alg": alg_tf / bf16, "frac_executed": exe / bf16,
+                         "executed": "%d plane products per entry and RHS (tile padding not "
+                                     "counted)" % TC_PRODUCTS[prec]}
+        if exe / bf16 > ach / hbm:
+            out.update({"bound": "tensor", "achieved": alg_tf, "peak": bf16, "unit": "TFLOP/s",
+                        "frac": alg_tf / bf16})
+    return out
 
 
 def timed(fac, X, Y, R, prec, steps, warmup, stream, dist):
@@ -813,7 +843,10 @@ def fac_summary(fac, wall_s):
             "jacobi_not_converged": st["jacobiNotConverged"],
             "sketched_blocks": st["numSketched"], "sketch_ms": st["sketchMs"],
             "sketch_mean_width": st["sketchMeanWidth"], "sketch_max_width": st["sketchMaxWidth"],
-            "sketch_retries": st["sketchRetries"], "fill_ms": st["fillMs"],
+            "sketch_retries": st["sketchRetries"],
+            "sketch_phase_ms": dict(zip(("fill", "z_omega", "qr_y", "zh_q", "qr_g", "jacobi",
+                                         "weights", "output"), st["sketchPhaseMs"])),
+            "fill_ms": st["fillMs"],
             "reexp_shared_ms": st["reexpSmemMs"], "reexp_global_ms": st["reexpGlobalMs"],
             "work": factorization_work(fac.block_table(), st)}
 

@@ -75,7 +75,7 @@ class _FacStatsC(ctypes.Structure):
         (n, ctypes.c_int64) for n in (
             "numSketched", "sketchRetries", "sketchFallbacks", "sketchMaxWidth")] + [
         (n, ctypes.c_double) for n in ("sketchMs", "sketchMeanWidth")] + [
-        ("applyBufferBytes", ctypes.c_int64)]
+        ("applyBufferBytes", ctypes.c_int64), ("sketchPhaseMs", ctypes.c_double * 8)]
 
 
 class _RngC(ctypes.Structure):
@@ -413,7 +413,9 @@ class Fac:
     def stats(self) -> dict:
         s = _FacStatsC()
         self.ctx.check(lib().bfgFacGetStats(self.handle, ctypes.byref(s)))
-        return {name: getattr(s, name) for name, _ in s._fields_}
+        out = {name: getattr(s, name) for name, _ in s._fields_}
+        out["sketchPhaseMs"] = list(out["sketchPhaseMs"])
+        return out
 
     def describe(self) -> str:
         n = _I64()

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <new>
 #include <stdexcept>
@@ -132,9 +133,16 @@ struct bfgFac_s {
   // chunk schedule of the 128-row program and the bf16 planes of the factors
   struct Tc {
     bool ready = false;
-    int32_t ctas = 0;
+    int32_t ctas = 0;                 // resident CTAs on the device
     size_t stages = 0;
-    DevBuf chunks, ctaChunk0, arena;
+    DevBuf arena;
+    bfg::ApplyProgram p128;           // the 128-row program the chunks cut
+    // chunk dealings by number of chunk streams: R right-hand sides take
+    // ctas / ceil(R / 16) streams (every tile of every stream resident)
+    struct Sched {
+      DevBuf chunks, ctaChunk0;
+    };
+    std::map<int32_t, Sched> sched;
   } tc[2];
   DevBuf tcStatus;                  // kStatusTcTimeout from the tensor-core kernel
   // the inputs (original order), kept for bfgFacSave; k holds one
@@ -402,6 +410,7 @@ void factorize(bfgFac f) {
     f->stats.sketchMaxWidth = rep.maxWidth;
     f->stats.sketchMs = rep.ms;
     f->stats.sketchMeanWidth = rep.blocks ? (double)rep.sumWidth / (double)rep.blocks : 0.0;
+    for (int i = 0; i < 8; ++i) f->stats.sketchPhaseMs[i] = rep.phaseMs[i];
     if (rep.notConverged) f->stats.jacobiNotConverged = 1;
   }
   ck(cudaEventRecord(eSketch, s), "event");
@@ -639,14 +648,15 @@ void ensureTc(bfgFac f, int terms) {
   int sms = 0;
   ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, f->ctx->device), "device");
   if (perSm < 1) throw BfgError{BFG_ERROR_RUNTIME, "tensor-core apply: kernel does not fit an SM"};
-  bfg::ApplyProgram p128;
+  bfg::ApplyProgram &p128 = tc.p128;
   bfg::makeApplyProgram(f->plan, p128, bfg::kTcRows);
   if (p128.wsRows != f->prog.wsRows || p128.stageItem0.size() != f->stageItem0.size())
     throw BfgError{BFG_ERROR_RUNTIME, "tensor-core apply: program mismatch"};
   bfg::TcSchedule sc;
   bfg::makeTcSchedule(p128, terms, perSm * sms, sc);
-  upload(tc.chunks, sc.chunks, s, "tensor-core schedule");
-  upload(tc.ctaChunk0, sc.ctaChunk0, s, "tensor-core schedule");
+  bfgFac_s::Tc::Sched &def = tc.sched[sc.ctas];
+  upload(def.chunks, sc.chunks, s, "tensor-core schedule");
+  upload(def.ctaChunk0, sc.ctaChunk0, s, "tensor-core schedule");
   DevBuf fills;
   upload(fills, sc.fills, s, "tensor-core schedule");
   ck(tc.arena.ensure((size_t)std::max<int64_t>(16, sc.arenaBytes)), "tensor-core factors");
@@ -677,11 +687,34 @@ void checkTcStatus(bfgFac f) {
   }
 }
 
+// chunk streams for R right-hand sides: the resident CTAs shared out over
+// the ceil(R / 16) tiles of every stream
+int32_t tcStreams(bfgFac_s::Tc const &tc, int64_t R) {
+  int64_t const tiles = (R + bfg::kTcRhsTile - 1) / bfg::kTcRhsTile;
+  return (int32_t)std::max<int64_t>(1, tc.ctas / std::max<int64_t>(1, tiles));
+}
+
+// the default dealing of the chunks to `streams` streams (built once)
+bfgFac_s::Tc::Sched &tcSched(bfgFac f, int terms, int32_t streams) {
+  bfgFac_s::Tc &tc = f->tc[terms - 2];
+  auto it = tc.sched.find(streams);
+  if (it != tc.sched.end()) return it->second;
+  bfg::TcSchedule sc;
+  bfg::makeTcSchedule(tc.p128, terms, streams, sc);
+  bfgFac_s::Tc::Sched &d = tc.sched[streams];
+  upload(d.chunks, sc.chunks, f->ctx->stream, "tensor-core schedule");
+  upload(d.ctaChunk0, sc.ctaChunk0, f->ctx->stream, "tensor-core schedule");
+  ck(cudaStreamSynchronize(f->ctx->stream), "tensor-core schedule");
+  return d;
+}
+
 void runApplyTc(bfgFac f, int terms, float2 const *X, int64_t ldx, int64_t R, float2 *Y,
                 int64_t ldy, uint32_t flags, std::vector<cudaEvent_t> *events) {
   cudaStream_t s = f->ctx->stream;
   bfg::ApplyProgram const &p = f->prog;
   bfgFac_s::Tc &tc = f->tc[terms - 2];
+  int32_t const streams = tcStreams(tc, R);
+  bfgFac_s::Tc::Sched &sched = tcSched(f, terms, streams);
   ck(f->ws.ensure((size_t)std::max<int64_t>(1, p.wsRows) * R * sizeof(float2)), "workspace");
   float2 *W = f->ws.as<float2>();
   float2 const *Xt = X;
@@ -701,8 +734,8 @@ void runApplyTc(bfgFac f, int terms, float2 const *X, int64_t ldx, int64_t R, fl
     mark();
   }
   for (size_t st = 0; st < tc.stages; ++st) {
-    ck(bfg::launchApplyTc(terms, tc.chunks.as<bfg::TcChunk>(),
-                          tc.ctaChunk0.as<int64_t>() + st * (size_t)(tc.ctas + 1), tc.ctas,
+    ck(bfg::launchApplyTc(terms, sched.chunks.as<bfg::TcChunk>(),
+                          sched.ctaChunk0.as<int64_t>() + st * (size_t)(streams + 1), streams,
                           tc.arena.as<uint8_t>(), Xt, ldxt, W, R, f->tcStatus.as<int32_t>(), s),
        "tensor-core apply stage");
     mark();
@@ -1394,10 +1427,9 @@ bfgStatus bfgFacAutotune(bfgFac f, bfgPrecision prec, int64_t R, double *stageMs
     ensureTc(f, terms);
     bfgFac_s::Tc &tc = f->tc[terms - 2];
     cudaStream_t s = f->ctx->stream;
-    bfg::ApplyProgram p128;
-    bfg::makeApplyProgram(f->plan, p128, bfg::kTcRows);
+    bfg::ApplyProgram const &p128 = tc.p128;
     size_t const nStages = tc.stages;
-    int32_t const ctas = tc.ctas;
+    int32_t const ctas = tcStreams(tc, R);
     std::vector<bfg::TcCostModel> const models = bfg::tcCandidateModels();   // default first
     size_t const K = models.size();
     std::vector<bfg::TcSchedule> cands(K);
@@ -1459,8 +1491,9 @@ bfgStatus bfgFacAutotune(bfgFac f, bfgPrecision prec, int64_t R, double *stageMs
       }
     }
     if (numStages) *numStages = (int32_t)nStages;
-    upload(tc.chunks, chunks, s, "tensor-core schedule");
-    upload(tc.ctaChunk0, c0, s, "tensor-core schedule");
+    bfgFac_s::Tc::Sched &tuned = tc.sched[ctas];
+    upload(tuned.chunks, chunks, s, "tensor-core schedule");
+    upload(tuned.ctaChunk0, c0, s, "tensor-core schedule");
     ck(cudaStreamSynchronize(s), "tensor-core schedule");
     return BFG_OK;
   });

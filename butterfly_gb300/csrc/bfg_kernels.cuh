@@ -78,6 +78,9 @@ struct SketchReport {
   int64_t maxWidth = 0, sumWidth = 0;
   int32_t notConverged = 0;
   double ms = 0.0;         // device time of the whole path
+  // device time per phase: fill, Y = Z Omega, qr(Y), G = Z^H Q, qr(G),
+  // Jacobi, weights (+ capture check), output GEMMs
+  double phaseMs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 // initial sketch width: widthScale * k r1 r2 / R + widthPad rounded up to 32,
 // at most m (R: distance of the equivalent and check circles' centres)
@@ -146,8 +149,11 @@ int32_t tcSmemBytes(int32_t terms);
 cudaError_t tcPrepare(int32_t terms, int32_t *ctasPerSm);
 cudaError_t launchTcFill(int32_t terms, TcFill const *fills, int64_t nFills,
                          double2 const *arena64, uint8_t *tarena, cudaStream_t stream);
-// one stage: `ctas` persistent CTAs (x) times RHS tiles of 16 (y); CTA c runs
-// chunks [ctaChunk0[c], ctaChunk0[c+1]); status bit 4 = a bounded wait expired
+// one stage: `ctas` chunk streams times ceil(R / 16) RHS tiles, one
+// persistent CTA each, the tiles of a stream adjacent in the grid; stream c
+// runs chunks [ctaChunk0[c], ctaChunk0[c+1]); status bit 4 = a bounded wait
+// expired
+constexpr int32_t kTcRhsTile = 16;
 cudaError_t launchApplyTc(int32_t terms, TcChunk const *chunks, int64_t const *ctaChunk0,
                           int32_t ctas, uint8_t const *tarena, float2 const *X, int64_t ldx,
                           float2 *W, int64_t R, int32_t *status, cudaStream_t stream);

@@ -708,6 +708,18 @@ cudaError_t runSketchReexpansion(std::vector<SketchInput> const &in, PointsDev s
   } evs{e0, e1};
   cudaEventRecord(e0, s);
 
+  // phase boundaries of each batch (timed after the batch's final sync)
+  struct PhaseEvents {
+    cudaEvent_t e[9] = {};
+    ~PhaseEvents() {
+      for (cudaEvent_t x : e)
+        if (x) cudaEventDestroy(x);
+    }
+  } pev;
+  for (cudaEvent_t &x : pev.e)
+    if ((err = cudaEventCreate(&x)) != cudaSuccess) return err;
+  auto mark = [&](int i) { cudaEventRecord(pev.e[i], s); };
+
   std::vector<SketchInput> queue = in;
   // largest first, so that the longest blocks start in the first wave
   auto cost = [](SketchInput const &a) { return (double)a.d.m * a.l * (a.l + a.d.m + a.d.n); };
@@ -768,6 +780,7 @@ cudaError_t runSketchReexpansion(std::vector<SketchInput> const &in, PointsDev s
     size_t const nb = blks.size();
 
     // fill
+    mark(0);
     std::vector<FillTileDesc> tiles;
     for (size_t i = 0; i < nb; ++i) {
       SketchDev const &b = blks[i];
@@ -793,11 +806,13 @@ cudaError_t runSketchReexpansion(std::vector<SketchInput> const &in, PointsDev s
     }
 
     // Y = Z Omega
+    mark(1);
     std::vector<GemmDesc> g;
     for (auto const &b : blks)
       g.push_back(GemmDesc{S + b.oZ, S + b.oB0, S + b.oB1, nullptr, b.p, b.p, b.p, b.p, b.l, b.p, 0});
     if ((err = launchGemms(g, dDesc, dTiles, s)) != cudaSuccess) return err;
     // Q = qr(Y) into B0
+    mark(2);
     std::vector<HqrDesc> h1, h2;
     for (auto const &b : blks) {
       HqrDesc h{S + b.oB1, S + b.oB0, S + b.oTau, nullptr, b.p, b.l};
@@ -806,11 +821,13 @@ cudaError_t runSketchReexpansion(std::vector<SketchInput> const &in, PointsDev s
     if ((err = launchHqr<1>(h1, dHqr1, s)) != cudaSuccess) return err;
     if ((err = launchHqr<2>(h2, dHqr2, s)) != cudaSuccess) return err;
     // G = Z^H Q into B1
+    mark(3);
     g.clear();
     for (auto const &b : blks)
       g.push_back(GemmDesc{S + b.oZ, S + b.oB0, S + b.oB1, nullptr, b.p, b.p, b.p, b.p, b.l, b.p, 1});
     if ((err = launchGemms(g, dDesc, dTiles, s)) != cudaSuccess) return err;
     // G = Q2 R2: Q2 into B2, [R2^H ; I] into M
+    mark(4);
     h1.clear();
     h2.clear();
     for (auto const &b : blks) {
@@ -820,6 +837,7 @@ cudaError_t runSketchReexpansion(std::vector<SketchInput> const &in, PointsDev s
     if ((err = launchHqr<1>(h1, dHqr1, s)) != cudaSuccess) return err;
     if ((err = launchHqr<2>(h2, dHqr2, s)) != cudaSuccess) return err;
     // Jacobi on [R2^H ; I]
+    mark(5);
     std::vector<JacobiDesc> j1, j2;
     for (auto const &b : blks) {
       JacobiDesc j{};
@@ -834,6 +852,7 @@ cudaError_t runSketchReexpansion(std::vector<SketchInput> const &in, PointsDev s
     if ((err = launchJacobi<1>(j1, dJac1, status, s)) != cudaSuccess) return err;
     if ((err = launchJacobi<2>(j2, dJac2, status, s)) != cudaSuccess) return err;
     // weights and capture
+    mark(6);
     std::vector<WeightDesc> wd;
     for (auto const &b : blks) {
       double *sw = reinterpret_cast<double *>(S + b.oSW);
@@ -881,12 +900,19 @@ cudaError_t runSketchReexpansion(std::vector<SketchInput> const &in, PointsDev s
       rep->maxWidth = std::max<int64_t>(rep->maxWidth, b.l);
       rep->sumWidth += b.l;
     }
+    mark(7);
     if ((err = launchGemms(gc, dDesc, dTiles, s)) != cudaSuccess) return err;
     if ((err = launchGemms(gd, dDesc, dTiles, s)) != cudaSuccess) return err;
     if ((err = launchGemms(ge, dDesc, dTiles, s)) != cudaSuccess) return err;
     if ((err = launchGemms(gx, dDesc, dTiles, s)) != cudaSuccess) return err;
+    mark(8);
     // descriptors and scratch are reused by the next batch
     if ((err = cudaStreamSynchronize(s)) != cudaSuccess) return err;
+    for (int i = 0; i < 8; ++i) {
+      float pm = 0.f;
+      cudaEventElapsedTime(&pm, pev.e[i], pev.e[i + 1]);
+      rep->phaseMs[i] += pm;
+    }
     queue.insert(queue.end(), requeue.begin(), requeue.end());
     q0 = q1;
   }

@@ -276,16 +276,21 @@ template <int TERMS>
 __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
     TcChunk const *__restrict__ chunks, int64_t const *__restrict__ ctaChunk0,
     uint8_t const *__restrict__ tarena, float2 const *__restrict__ X, int64_t ldx,
-    float2 *__restrict__ W, int64_t R, int32_t xBulk, int32_t *status) {
+    float2 *__restrict__ W, int64_t R, int32_t rhsTiles, int32_t xBulk, int32_t *status) {
   using L = TcLayout<TERMS>;
   constexpr int S = kTcStages;
   constexpr int kBKGroupBytes = L::kBKGroupBytes;
   extern __shared__ __align__(1024) uint8_t smem[];
   int const tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  int64_t const c0 = ctaChunk0[blockIdx.x];
-  int64_t const nCh = ctaChunk0[blockIdx.x + 1] - c0;
+  // CTA = (chunk stream, RHS tile), the tile varying fastest: the tiles of a
+  // stream run side by side and read each A chunk from HBM once, the other
+  // tiles finding it in L2
+  int const stream = (int)(blockIdx.x / (unsigned)rhsTiles);
+  int const tile = (int)(blockIdx.x % (unsigned)rhsTiles);
+  int64_t const c0 = ctaChunk0[stream];
+  int64_t const nCh = ctaChunk0[stream + 1] - c0;
   if (nCh <= 0) return;
-  int64_t const r0 = (int64_t)blockIdx.y * kTcRhs;
+  int64_t const r0 = (int64_t)tile * kTcRhs;
   int const nr = (R - r0) < kTcRhs ? (int)(R - r0) : kTcRhs;
   TcChunk const *ch = chunks + c0;
   // a chunk's right-hand sides arrive by one bulk copy with its A planes when
@@ -669,16 +674,18 @@ cudaError_t launchApplyTc(int32_t terms, TcChunk const *chunks, int64_t const *c
                           int32_t ctas, uint8_t const *tarena, float2 const *X, int64_t ldx,
                           float2 *W, int64_t R, int32_t *status, cudaStream_t stream) {
   if (ctas == 0) return cudaSuccess;
-  dim3 grid((unsigned)ctas, (unsigned)((R + kTcRhs - 1) / kTcRhs));
+  int64_t const tiles = (R + kTcRhs - 1) / kTcRhs;
+  if (tiles > 0x7fffffff / ctas) return cudaErrorInvalidValue;
+  dim3 grid((unsigned)(ctas * tiles));
   // one bulk copy per chunk: 16 RHS with leading dimension 16, 16-byte aligned
   int32_t const xBulk = ((R == kTcRhs && ldx == kTcRhs && (uintptr_t)X % 16 == 0) ? kTcBulkX : 0) |
                         ((R == kTcRhs && (uintptr_t)W % 16 == 0) ? kTcBulkW : 0);
   if (terms == 3)
-    applyTcKernel<3><<<grid, kTcThreads, TcLayout<3>::smemBytes, stream>>>(chunks, ctaChunk0, tarena, X,
-                                                                     ldx, W, R, xBulk, status);
+    applyTcKernel<3><<<grid, kTcThreads, TcLayout<3>::smemBytes, stream>>>(
+        chunks, ctaChunk0, tarena, X, ldx, W, R, (int32_t)tiles, xBulk, status);
   else
-    applyTcKernel<2><<<grid, kTcThreads, TcLayout<2>::smemBytes, stream>>>(chunks, ctaChunk0, tarena, X,
-                                                                     ldx, W, R, xBulk, status);
+    applyTcKernel<2><<<grid, kTcThreads, TcLayout<2>::smemBytes, stream>>>(
+        chunks, ctaChunk0, tarena, X, ldx, W, R, (int32_t)tiles, xBulk, status);
   return cudaGetLastError();
 }
 

@@ -133,6 +133,9 @@ typedef struct bfgFacStats {
   int64_t applyBufferBytes;   /* device bytes the allocating applies have
                                  allocated so far (workspace and gather
                                  buffers; bfgFacApplyNoAlloc adds none) */
+  double sketchPhaseMs[8];    /* randomized path by phase: fills, Z Omega,
+                                 qr(Y), Z^H Q, qr(G), Jacobi, weights and
+                                 capture test, output products */
 } bfgFacStats;
 
 /* Contexts: one CUDA device and one stream; calls on a context are
