@@ -276,10 +276,10 @@ constexpr int32_t kClusterMinRank = 128;
 // the randomized re-expansion path: blocks from this rank estimate whose
 // initial sketch is at most kSketchMaxFraction of it; the sketch width is
 // kSketchWidthScale k r1 r2 / R + kSketchWidthPad; scratch per batch
-constexpr int32_t kSketchMinRank = 256;
-constexpr double kSketchMaxFraction = 0.6;
-constexpr double kSketchWidthScale = 1.15;
-constexpr int32_t kSketchWidthPad = 48;
+constexpr int32_t kSketchMinRank = 128;
+constexpr double kSketchMaxFraction = 0.8;
+constexpr double kSketchWidthScale = 1.1;
+constexpr int32_t kSketchWidthPad = 40;
 constexpr int64_t kSketchBudgetEntries = (int64_t)1 << 30;   // 16 GiB of complex128
 // LAST and DENSE blocks are filled in column pieces of at most this many
 // columns and entries, so that one large block spreads over many CTAs

@@ -87,7 +87,7 @@ struct SketchReport {
 int32_t sketchWidth(FillDesc const &d, double widthScale, int32_t widthPad);
 // Computes the blocks of `in` into the arena.  A block whose sketch missed
 // part of Z_equiv's numerical rank (smallest sigma above capture * sigma0) is
-// sketched again with twice the width, or, when that width passes 0.6 m and
+// sketched again with twice the width, or, when that width passes 0.8 m and
 // the full path can take it, appended to *fallback.  Scratch is allocated per
 // batch of blocks within budgetEntries complex entries (at least one block).
 cudaError_t runSketchReexpansion(std::vector<SketchInput> const &in, PointsDev src,

@@ -881,7 +881,7 @@ cudaError_t runSketchReexpansion(std::vector<SketchInput> const &in, PointsDev s
         SketchInput r = src1;
         r.l = std::min<int32_t>(b.p, 2 * b.l);
         ++rep->retries;
-        if (r.fullOk && r.l > (int32_t)(0.6 * b.p)) {
+        if (r.fullOk && r.l > (int32_t)(0.8 * b.p)) {
           fallback->push_back(r.d);
           ++rep->fallbacks;
         } else {

@@ -96,7 +96,7 @@ typedef struct bfgFacOptions {
                           value, so it requires pinvCut = 1 with
                           pinvTol >= 1e-10 */
   int32_t sketch;     /* 1 (default): a FIRST/MIDDLE block of rank estimate
-                         p >= 256 whose Z_equiv has a numerical rank well
+                         p >= 128 whose Z_equiv has a numerical rank well
                          below p (about k r1 r2 / R against the estimate's
                          k r1 r2 / (R - r1 - r2)) takes the randomized range
                          finder instead of the p x p Jacobi SVD, when

@@ -698,7 +698,7 @@ def lstsq_pinv(A: np.ndarray, B: np.ndarray, rcut: str = "reference",
     return (X, k, S) if return_terms else X
 
 
-def sketch_width(k: float, ceq, cchk, m: int, scale: float = 1.15, pad: int = 48) -> int:
+def sketch_width(k: float, ceq, cchk, m: int, scale: float = 1.1, pad: int = 40) -> int:
     """Initial width of the library's randomized re-expansion for a block
     with rank estimate m: scale * k r1 r2 / R + pad rounded up to 32, at most
     m (R: distance of the equivalent and check circles' centres).  The rank

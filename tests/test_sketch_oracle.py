@@ -23,7 +23,7 @@ def _blocks(N, k, curve, eps, leaf=64):
         if b.kind not in ("first", "middle") or b.m < 256:
             continue
         w = O.sketch_width(k, b.ceq, b.cchk, b.m)
-        if w <= 0.6 * b.m:
+        if w <= 0.5 * b.m:
             out.append((b, w))
     return out, src_tree_pts
 
