@@ -89,7 +89,10 @@ def factorization_work(table, st):
     svd = float(np.sum(22.0 * m[fm] ** 3 + 16.0 * m[fm] ** 2 * n[fm]))
     reexp_s = (st["reexpSmemMs"] + st["reexpGlobalMs"]) / 1e3
     tflops = svd / reexp_s / 1e12 if reexp_s > 0 else None
+    meas = FP64_MEASURED["tflops"]
     return {"kernel_evals": fill + proxy, "fill_evals": fill, "proxy_evals": proxy,
+            "fp64_measured_tflops": meas,
+            "frac_of_measured_fp64": tflops / meas if tflops and meas else None,
             "fill_evals_per_s": fill / (st["fillMs"] / 1e3) if st["fillMs"] > 0 else None,
             "svd_flops_model": svd,
             "svd_model": "22 p^3 + 16 p^2 n per FIRST/MIDDLE block (rank p, n columns)",
@@ -856,6 +859,9 @@ def rel_rows(Y, rows, Re, yd):
     return float(np.linalg.norm(ye - yd) / np.linalg.norm(yd))
 
 
+FP64_MEASURED = {"tflops": None}
+
+
 def small_rhs_block(B, fac, ctx, stream, n, R, precs, steps, yd_rows, Xh, dist):
     """Applies to R (1 or few) right-hand sides: RHS/s, error against the
     oracle rows, and the dominant launch's HBM roofline per precision."""
@@ -875,11 +881,14 @@ def small_rhs_block(B, fac, ctx, stream, n, R, precs, steps, yd_rows, Xh, dist):
         err = rel_rows(Y, rows, R, yd[:, :R]) if yd is not None else None
         tot, med, _ = timed(fac, X, Y, R, p, steps, 3, stream, dist)
         roof = launch_roofline(fac, X, Y, R, p)
+        tf = float(fac.stats()["flopsPerRhs"] * R / (tot / steps / 1e3) / 1e12)
         out[p] = {"rhs_per_s": R * steps / (tot / 1e3), "ms_per_apply": tot / steps,
-                  "rel_err": err, "dominant_launch_gbs": roof["achieved"],
-                  "dominant_launch_frac_of_measured_hbm": roof["frac"],
+                  "rel_err": err, "dominant_launch_gbs": roof["hbm"]["achieved_gbs"],
+                  "dominant_launch_frac_of_measured_hbm": roof["hbm"]["frac"],
                   "whole_apply_gbs": roof["whole_apply_gbs"],
-                  "whole_apply_tflops": float(fac.stats()["flopsPerRhs"] * R / (tot / steps / 1e3) / 1e12)}
+                  "whole_apply_tflops": tf}
+        if p == "fp64" and FP64_MEASURED["tflops"]:
+            out[p]["whole_apply_frac_of_measured_fp64"] = tf / FP64_MEASURED["tflops"]
     return out
 
 
@@ -941,6 +950,8 @@ def main():
     R = args.rhs or cfg["R"]
     n = cfg["n"]
     ctx = B.Context(local)
+    # the FP64 roof of the FP64 apply and the factorization, measured here
+    FP64_MEASURED["tflops"] = B.measure_fp64_rate(ctx)
     src, tgt = workload_inputs(cfg, "bfg")
     fac, fac_wall_s = make_fac(B, ctx, cfg, src, tgt)
     sp, tp = fac.perms()
@@ -1121,7 +1132,8 @@ def main():
             "factorization": fac_info, "rhs1": rhs1,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": launches, "gmres": gm, "autotune": tuned,
-            "cpu_factorization": cpu_fac, "c2": c2}
+            "cpu_factorization": cpu_fac, "c2": c2,
+            "fp64_measured_tflops": FP64_MEASURED["tflops"]}
     print(json.dumps(line))
 
 

@@ -128,6 +128,7 @@ def lib() -> ctypes.CDLL:
         "bfgHelm2KernelMatrix": [_VP, ctypes.POINTER(_Helm2C), _VP, _VP, _I64, _VP, _VP, _I64,
                                  _VP],
         "bfgBessel01": [_VP, _VP, _I64, _VP],
+        "bfgMeasureFp64Rate": [_VP, ctypes.POINTER(ctypes.c_double)],
         "bfgPlanHelm2": [ctypes.c_double, _VP, _I64, _VP, _I64, ctypes.POINTER(_FacOptionsC),
                          _VP, _VP, ctypes.c_char_p, _I64, ctypes.POINTER(_I64)],
         "bfgBessel01Host": [_VP, _I64, _VP],
@@ -545,6 +546,14 @@ def kernel_matrix(helm: Helm2, src, tgt, src_normals=None, tgt_normals=None,
                                          len(src), _ptr(tgt), _ptr(tn), len(tgt), _ptr(out)),
               "kernel_matrix")
     return out
+
+
+def measure_fp64_rate(context: Context | None = None) -> float:
+    """The device's measured FP64 FMA rate in TFLOP/s (bfgMeasureFp64Rate)."""
+    ctx = context or default_context()
+    v = ctypes.c_double()
+    ctx.check(lib().bfgMeasureFp64Rate(ctx.handle, ctypes.byref(v)), "measure_fp64_rate")
+    return float(v.value)
 
 
 def bessel01(x, context: Context | None = None) -> np.ndarray:

@@ -1662,6 +1662,30 @@ bfgStatus bfgBessel01(bfgContext ctx, double const *x, int64_t n, double *out) {
   });
 }
 
+bfgStatus bfgMeasureFp64Rate(bfgContext ctx, double *tflops) {
+  if (!ctx || !tflops) return BFG_ERROR_INVALID_ARGUMENTS;
+  return guarded(ctx, [&]() -> bfgStatus {
+    cudaStream_t s = ctx->stream;
+    int sms = 0;
+    ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device), "device");
+    int32_t const blocks = 8 * sms;
+    DevBuf out;
+    ck(out.ensure((size_t)blocks * sizeof(double)), "fp64 rate");
+    Events const ev(2, "fp64 rate");
+    ck(bfg::launchFp64Rate(blocks, 1024, out.as<double>(), s), "fp64 rate");   // warm-up
+    int32_t const iters = 4096;
+    ck(cudaEventRecord(ev[0], s), "fp64 rate");
+    ck(bfg::launchFp64Rate(blocks, iters, out.as<double>(), s), "fp64 rate");
+    ck(cudaEventRecord(ev[1], s), "fp64 rate");
+    ck(cudaEventSynchronize(ev[1]), "fp64 rate");
+    float ms = 0;
+    ck(cudaEventElapsedTime(&ms, ev[0], ev[1]), "fp64 rate");
+    double const flops = 2.0 * 8.0 * iters * 256.0 * blocks;
+    *tflops = flops / (ms * 1e-3) / 1e12;
+    return BFG_OK;
+  });
+}
+
 bfgStatus bfgPlanHelm2(double k, double const *srcXy, int64_t numSrc, double const *tgtXy,
                        int64_t numTgt, bfgFacOptions const *opts, int64_t *srcPerm,
                        int64_t *tgtPerm, char *buf, int64_t cap, int64_t *len) {

@@ -633,6 +633,22 @@ __global__ void kernelMatrixKernel(PointsDev src, int64_t n, PointsDev tgt, int6
   }
 }
 
+// FP64 fused multiply-add throughput: 8 independent chains per thread, the
+// result written so that nothing is optimised away
+__global__ void __launch_bounds__(256) fp64RateKernel(int32_t iters, double seed, double *out) {
+  double a[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) a[c] = seed + 1e-3 * (threadIdx.x + 8 * c);
+  double const b = 0.9999999, d = 1e-9;
+  for (int i = 0; i < iters; ++i)
+#pragma unroll
+    for (int c = 0; c < 8; ++c) a[c] = fma(a[c], b, d);
+  double t = 0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) t += a[c];
+  if (t == 12345.678) out[blockIdx.x] = t;   // never true for these inputs
+}
+
 __global__ void bessel01Kernel(double const *x, int64_t n, double *out) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -1128,6 +1144,11 @@ cudaError_t launchKernelMatrix(PointsDev src, int64_t n, PointsDev tgt, int64_t 
                                KernelParams kp, double2 *out, cudaStream_t stream) {
   if (m * n == 0) return cudaSuccess;
   kernelMatrixKernel<<<gridFor(m * n, 256), 256, 0, stream>>>(src, n, tgt, m, kp, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launchFp64Rate(int32_t blocks, int32_t iters, double *out, cudaStream_t stream) {
+  fp64RateKernel<<<(unsigned)blocks, 256, 0, stream>>>(iters, 0.5, out);
   return cudaGetLastError();
 }
 

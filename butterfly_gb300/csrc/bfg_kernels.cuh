@@ -105,6 +105,9 @@ cudaError_t launchDenseRows(PointsDev src, int64_t nSrc, PointsDev tgt,
 cudaError_t launchKernelMatrix(PointsDev src, int64_t n, PointsDev tgt, int64_t m,
                                KernelParams kp, double2 *out, cudaStream_t stream);
 
+// FP64 FMA throughput probe: blocks x 256 threads x iters x 8 FMAs
+cudaError_t launchFp64Rate(int32_t blocks, int32_t iters, double *out, cudaStream_t stream);
+
 // H0, H1 at x[i]: out[4i..4i+3] = J0, Y0, J1, Y1
 cudaError_t launchBessel01(double const *x, int64_t n, double *out, cudaStream_t stream);
 

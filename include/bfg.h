@@ -302,6 +302,12 @@ bfgStatus bfgHelm2KernelMatrix(bfgContext ctx, bfgHelm2 const *helm,
  * out[4i..4i+3] = J0, Y0, J1, Y1 at x[i] > 0 (host arrays). */
 bfgStatus bfgBessel01(bfgContext ctx, double const *x, int64_t n, double *out);
 
+/* The device's FP64 fused multiply-add rate in TFLOP/s (2 flops per FMA),
+ * measured with CUDA events on a kernel of independent FMA chains over all
+ * SMs (~100 ms): the FP64 roof of the FP64 apply and the factorization.  No
+ * counterpart in the reference. */
+bfgStatus bfgMeasureFp64Rate(bfgContext ctx, double *tflops);
+
 /* ---------------------------------------------------------------------
  * Boundary-integral systems and GMRES
  * --------------------------------------------------------------------- */

@@ -210,6 +210,13 @@ def test_dense_rows_on_gpu_match_oracle_at_higher_wavenumber(ctx):
     assert rel_err(yg, yo) < 1e-12
 
 
+def test_fp64_rate_probe(ctx):
+    """bfgMeasureFp64Rate, the FP64 roof the bench reports beside the FP64
+    kernels: a positive rate of the order of GB300's nominal 1.25 TFLOP/s."""
+    r = B.measure_fp64_rate(ctx)
+    assert 0.2 < r < 20.0
+
+
 def test_tolerance_and_leaf_options_against_dense(ctx):
     """The workloads' knobs (leaf size, rank tolerance, relative pseudo-
     inverse cut) trade accuracy for size; the result is checked against the
