@@ -119,6 +119,9 @@ def parse():
                     help="skip the 65,536-point workload's block (1 and 16 RHS)")
     ap.add_argument("--no-cpu-factorization", action="store_true",
                     help="skip the oracle factorization timings on the host cores")
+    ap.add_argument("--profile", default="", choices=["", "fp64", "df64", "fp32", "bf16x3", "bf16x2"],
+                    help="profiling driver: factorize the workload, then run --warmup + --steps "
+                         "applies of this precision to --rhs RHS with no timing (for ncu)")
     ap.add_argument("--cpu-fac-worker", default="", help=argparse.SUPPRESS)
     ap.add_argument("--cpu-fac-budget", type=float, default=0.0, help=argparse.SUPPRESS)
     ap.add_argument("--no-gmres", action="store_true",
@@ -316,12 +319,14 @@ def run_batched(args, cfg):
         Y32 = torch.empty((n, R), dtype=torch.complex64, device="cuda")
     stream.synchronize()
     precs = {"fp64": (X64, Y64), "fp32": (X32, Y32), "bf16x3": (X32, Y32), "bf16x2": (X32, Y32)}
-    # dense FP64 rows of 8 sampled problems (64 target rows each)
+    # dense FP64 rows of 8 sampled problems (64 target rows each) from the
+    # oracle on the host cores (glibc Bessel functions, helm2.c:282-319)
+    from oracle import bf_oracle as O
     ref = []
     for j in range(0, len(problems), max(1, len(problems) // 8)):
         src, tgt = problems[j]
         rows = np.unique(np.linspace(0, len(tgt) - 1, 64).astype(np.int64))
-        K = B.kernel_matrix(B.Helm2(float(ks[j])), src, tgt[rows], context=ctx)
+        K = O.kernel_matrix(O.Helm2(float(ks[j])), src, tgt[rows])
         ref.append((to[j] + rows, K @ Xh[so[j]:so[j + 1]]))
     errs = {}
     for p, (X, Y) in precs.items():
@@ -388,7 +393,8 @@ def run_batched(args, cfg):
                        "l2": "factor arena and vectors larger than L2 (129 MB); no flush needed"},
             "precision": head, "rel_err": errs[head], "rel_err_all": errs,
             "rhs_per_s_all": rhs_s, "problem_rhs_per_s": rhs_s[head] * cfg["problems"],
-            "err_bound": ERR_BOUND, "err_sample": "64 rows of each of %d problems" % len(ref),
+            "err_bound": ERR_BOUND,
+            "err_sample": "64 rows of each of %d problems, oracle rows on the host" % len(ref),
             "factorization": {"wall_s": fac_s, "device_ms": st["factorMs"],
                               "blocks": st["numBlocks"], "bytes_fp64": fac.num_bytes(),
                               "max_rank": st["maxRank"],
@@ -923,8 +929,43 @@ def secondary_c2(B, ctx, stream, args, dist):
     return res
 
 
+def run_profile(args):
+    """--profile: the workload's factorization, then W + K applies of one
+    precision on device-resident operands, untimed, for an ncu capture of
+    the apply kernels (skip the factorization's and the warm-up applies'
+    launches with ncu -s)."""
+    import torch
+
+    import butterfly_gb300 as B
+    cfg = CONFIGS[args.config]
+    R = args.rhs or cfg["R"]
+    n = cfg["n"]
+    ctx = B.Context(0)
+    if args.profile in ("fp64", "df64"):
+        print(json.dumps({"fp64_measured_tflops": B.measure_fp64_rate(ctx)}), flush=True)
+    src, tgt = workload_inputs(cfg, "bfg")
+    fac, wall = make_fac(B, ctx, cfg, src, tgt)
+    dt = torch.complex128 if args.profile in ("fp64", "df64") else torch.complex64
+    X = torch.from_numpy(B.Rng(5).complex_randn(n * R).reshape(n, R)).to("cuda").to(dt)
+    Y = torch.empty_like(X)
+    torch.cuda.synchronize()
+    for _ in range(args.warmup + args.steps):
+        fac.apply_device(X.data_ptr(), R, R, Y.data_ptr(), R, args.profile)
+    torch.cuda.synchronize()
+    per = fac.apply_timed(X.data_ptr(), R, R, Y.data_ptr(), R, args.profile)
+    info = fac.launch_info()
+    print(json.dumps({"workload": args.config, "rhs": R, "precision": args.profile,
+                      "factorization_s": wall, "launches_per_apply": len(info),
+                      "entries_per_launch": [int(v) for v in info[:, 0]],
+                      "rows_in_out_per_launch": [[int(a), int(b)] for a, b in info[:, 1:]],
+                      "launch_ms": [float(v) for v in per]}))
+
+
 def main():
     args = parse()
+    if args.profile:
+        run_profile(args)
+        return
     if args.cpu_fac_worker:
         print(json.dumps(cpu_factorization_worker(args.cpu_fac_worker, args.cpu_fac_budget)))
         return

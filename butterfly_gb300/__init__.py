@@ -129,6 +129,7 @@ def lib() -> ctypes.CDLL:
                                  _VP],
         "bfgBessel01": [_VP, _VP, _I64, _VP],
         "bfgMeasureFp64Rate": [_VP, ctypes.POINTER(ctypes.c_double)],
+        "bfgFacSetTcWaitLimit": [_VP, ctypes.c_uint64],
         "bfgPlanHelm2": [ctypes.c_double, _VP, _I64, _VP, _I64, ctypes.POINTER(_FacOptionsC),
                          _VP, _VP, ctypes.c_char_p, _I64, ctypes.POINTER(_I64)],
         "bfgBessel01Host": [_VP, _I64, _VP],

@@ -145,6 +145,7 @@ struct bfgFac_s {
     std::map<int32_t, Sched> sched;
   } tc[2];
   DevBuf tcStatus;                  // kStatusTcTimeout from the tensor-core kernel
+  uint64_t tcWaitLimitNs = bfg::kTcWaitLimitNs;   // lowered only by the test hook
   // the inputs (original order), kept for bfgFacSave; k holds one
   // wavenumber per problem and the offsets are empty for a single problem
   std::vector<double> inSrcXy, inSrcN, inTgtXy, inTgtN, inK;
@@ -736,7 +737,8 @@ void runApplyTc(bfgFac f, int terms, float2 const *X, int64_t ldx, int64_t R, fl
   for (size_t st = 0; st < tc.stages; ++st) {
     ck(bfg::launchApplyTc(terms, sched.chunks.as<bfg::TcChunk>(),
                           sched.ctaChunk0.as<int64_t>() + st * (size_t)(streams + 1), streams,
-                          tc.arena.as<uint8_t>(), Xt, ldxt, W, R, f->tcStatus.as<int32_t>(), s),
+                          tc.arena.as<uint8_t>(), Xt, ldxt, W, R, f->tcStatus.as<int32_t>(), s,
+                          f->tcWaitLimitNs),
        "tensor-core apply stage");
     mark();
   }
@@ -1414,6 +1416,12 @@ bfgStatus bfgFacApplyHost(bfgFac f, bfgPrecision prec, double const *X, int64_t 
     if (isTcPrecision(prec)) checkTcStatus(f);
     return BFG_OK;
   });
+}
+
+bfgStatus bfgFacSetTcWaitLimit(bfgFac f, uint64_t waitLimitNs) {
+  if (!f) return BFG_ERROR_INVALID_ARGUMENTS;
+  f->tcWaitLimitNs = waitLimitNs;
+  return BFG_OK;
 }
 
 bfgStatus bfgFacAutotune(bfgFac f, bfgPrecision prec, int64_t R, double *stageMs,

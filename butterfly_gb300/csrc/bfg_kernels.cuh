@@ -157,9 +157,13 @@ cudaError_t launchTcFill(int32_t terms, TcFill const *fills, int64_t nFills,
 // runs chunks [ctaChunk0[c], ctaChunk0[c+1]); status bit 4 = a bounded wait
 // expired
 constexpr int32_t kTcRhsTile = 16;
+// every mbarrier wait of the kernel gives up after waitLimitNs (then the CTA
+// drains what it has in flight, frees its tensor memory and sets status bit 4)
+constexpr uint64_t kTcWaitLimitNs = 1000000000ull;
 cudaError_t launchApplyTc(int32_t terms, TcChunk const *chunks, int64_t const *ctaChunk0,
                           int32_t ctas, uint8_t const *tarena, float2 const *X, int64_t ldx,
-                          float2 *W, int64_t R, int32_t *status, cudaStream_t stream);
+                          float2 *W, int64_t R, int32_t *status, cudaStream_t stream,
+                          uint64_t waitLimitNs = kTcWaitLimitNs);
 enum : int32_t { kStatusTcTimeout = 4 };
 
 // X_tree[i] = X[perm[i]] (row gather, R columns)

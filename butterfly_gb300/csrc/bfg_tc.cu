@@ -113,14 +113,15 @@ __device__ __forceinline__ uint64_t globalTimerNs() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-// waits for the phase with the given parity; false after kWaitLimitNs or as
-// soon as another role of the CTA has given up (*abort set)
-__device__ bool mbarWait(uint32_t bar, uint32_t parity, int volatile *abort) {
+// waits for the phase with the given parity; false after limitNs (the
+// launch's wait limit, kWaitLimitNs unless a test lowers it) or as soon as
+// another role of the CTA has given up (*abort set)
+__device__ bool mbarWait(uint32_t bar, uint32_t parity, int volatile *abort, uint64_t limitNs) {
   if (mbarTryWait(bar, parity)) return true;
   uint64_t const t0 = globalTimerNs();
   for (;;) {
     if (mbarTryWait(bar, parity)) return true;
-    if (*abort || globalTimerNs() - t0 > kWaitLimitNs) return false;
+    if (*abort || globalTimerNs() - t0 > limitNs) return false;
   }
 }
 // the same wait without the early exit (draining work in flight)
@@ -276,7 +277,8 @@ template <int TERMS>
 __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
     TcChunk const *__restrict__ chunks, int64_t const *__restrict__ ctaChunk0,
     uint8_t const *__restrict__ tarena, float2 const *__restrict__ X, int64_t ldx,
-    float2 *__restrict__ W, int64_t R, int32_t rhsTiles, int32_t xBulk, int32_t *status) {
+    float2 *__restrict__ W, int64_t R, int32_t rhsTiles, int32_t xBulk, uint64_t waitLimitNs,
+    int32_t *status) {
   using L = TcLayout<TERMS>;
   constexpr int S = kTcStages;
   constexpr int kBKGroupBytes = L::kBKGroupBytes;
@@ -348,7 +350,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
         inIsXN = ch[i + 1].inIsX;
       }
       int ok = 1;
-      if (i >= S && lane == 0) ok = mbarWait(empty + 8 * s, (uint32_t)((i / S - 1) & 1), abortFlag);
+      if (i >= S && lane == 0) ok = mbarWait(empty + 8 * s, (uint32_t)((i / S - 1) & 1), abortFlag, waitLimitNs);
       if (!__shfl_sync(0xffffffffu, ok, 0)) {
         if (lane == 0) *abortFlag = 1;
         break;
@@ -398,8 +400,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
           kgN = ch[i + 2].kg;
           mgN = ch[i + 2].mg;
         }
-        if (!mbarWait(fullA + 8 * s, ph, abortFlag) || !mbarWait(fullB + 8 * s, ph, abortFlag) ||
-            (i >= 2 && !mbarWait(accEmpty + 8 * b, (uint32_t)(((i >> 1) - 1) & 1), abortFlag))) {
+        if (!mbarWait(fullA + 8 * s, ph, abortFlag, waitLimitNs) || !mbarWait(fullB + 8 * s, ph, abortFlag, waitLimitNs) ||
+            (i >= 2 && !mbarWait(accEmpty + 8 * b, (uint32_t)(((i >> 1) - 1) & 1), abortFlag, waitLimitNs))) {
           *abortFlag = 1;
           break;
         }
@@ -507,13 +509,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
         // others leave the loop, and the passing lanes' __syncwarp would
         // then wait forever for lanes already at the final barrier.
         if (bulkOf(d0) &&
-            !__all_sync(0xffffffffu, mbarWait(fullX + 8 * s, (uint32_t)((i / S) & 1), abortFlag))) {
+            !__all_sync(0xffffffffu, mbarWait(fullX + 8 * s, (uint32_t)((i / S) & 1), abortFlag, waitLimitNs))) {
           *abortFlag = 1;
           break;
         }
         if (i >= S &&
             !__all_sync(0xffffffffu,
-                        mbarWait(empty + 8 * s, (uint32_t)((i / S - 1) & 1), abortFlag))) {
+                        mbarWait(empty + 8 * s, (uint32_t)((i / S - 1) & 1), abortFlag, waitLimitNs))) {
           *abortFlag = 1;
           break;
         }
@@ -580,7 +582,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
         dn = loadCe(j + 1);
         int const b = (int)(j & 1);
         // as one warp (a vote), for the collective TMEM loads below
-        if (!__all_sync(0xffffffffu, mbarWait(accFull + 8 * b, (uint32_t)((j >> 1) & 1), abortFlag))) {
+        if (!__all_sync(0xffffffffu, mbarWait(accFull + 8 * b, (uint32_t)((j >> 1) & 1), abortFlag, waitLimitNs))) {
           *abortFlag = 1;
           break;
         }
@@ -672,7 +674,8 @@ cudaError_t launchTcFill(int32_t terms, TcFill const *fills, int64_t nFills,
 
 cudaError_t launchApplyTc(int32_t terms, TcChunk const *chunks, int64_t const *ctaChunk0,
                           int32_t ctas, uint8_t const *tarena, float2 const *X, int64_t ldx,
-                          float2 *W, int64_t R, int32_t *status, cudaStream_t stream) {
+                          float2 *W, int64_t R, int32_t *status, cudaStream_t stream,
+                          uint64_t waitLimitNs) {
   if (ctas == 0) return cudaSuccess;
   int64_t const tiles = (R + kTcRhs - 1) / kTcRhs;
   if (tiles > 0x7fffffff / ctas) return cudaErrorInvalidValue;
@@ -682,10 +685,10 @@ cudaError_t launchApplyTc(int32_t terms, TcChunk const *chunks, int64_t const *c
                         ((R == kTcRhs && (uintptr_t)W % 16 == 0) ? kTcBulkW : 0);
   if (terms == 3)
     applyTcKernel<3><<<grid, kTcThreads, TcLayout<3>::smemBytes, stream>>>(
-        chunks, ctaChunk0, tarena, X, ldx, W, R, (int32_t)tiles, xBulk, status);
+        chunks, ctaChunk0, tarena, X, ldx, W, R, (int32_t)tiles, xBulk, waitLimitNs, status);
   else
     applyTcKernel<2><<<grid, kTcThreads, TcLayout<2>::smemBytes, stream>>>(
-        chunks, ctaChunk0, tarena, X, ldx, W, R, (int32_t)tiles, xBulk, status);
+        chunks, ctaChunk0, tarena, X, ldx, W, R, (int32_t)tiles, xBulk, waitLimitNs, status);
   return cudaGetLastError();
 }
 

@@ -215,6 +215,15 @@ bfgStatus bfgFacCopyBlocks(bfgFac fac, double *entries, int64_t capacityEntries,
 /* Builds the precision's copy of the factors now, as the first apply in that
  * precision would (allocates and synchronises). */
 bfgStatus bfgFacPrepare(bfgFac fac, bfgPrecision precision);
+/* Test hook (no counterpart in the reference): the time after which every
+ * bounded wait of the tensor-core apply (BFG_PRECISION_BF16X2/X3) gives up,
+ * 1 s by default.  A wait that gives up makes each CTA drain its copies and
+ * tensor-core products in flight, free its tensor memory and end; the apply
+ * then returns BFG_ERROR_TIMEOUT and the factorization stays usable.  0
+ * makes every wait that is not already satisfied give up at once, which is
+ * how the tests drive that path. */
+bfgStatus bfgFacSetTcWaitLimit(bfgFac fac, uint64_t waitLimitNs);
+
 /* Autotuner of the tensor-core apply (BF16X2, BF16X3): deals each stage's
  * chunks to the persistent CTAs under several cost models, times every
  * stage of every candidate on the GPU (numRhs right-hand sides, best of 5)
