@@ -62,7 +62,8 @@ NCU_DRAM_PER_ALG = {("c2", "fp32", 16): [0.7973, 1.0266, 0.9855, 0.7925],
                     ("c2s", "fp32", 16): [0.7973, 1.0266, 0.9855, 0.7925],
                     ("c2s", "bf16x3", 16): [0.8888, 1.0627, 1.0246, 1.0386]}
 NCU_TRAFFIC_SOURCE = {
-    "c2": "ncu DRAM bytes of the same stage in the c2s capture, scaled by algorithmic bytes",
+    "c2": "ncu DRAM bytes of the same stage in a capture of the 32,768-point workload, "
+          "scaled by algorithmic bytes",
     "c2s": "ncu capture"}
 ERR_BOUND = 1e-6
 # GB300's dense FP64 rate (nominal; no measured FP64 peak is available)

@@ -49,6 +49,22 @@ __device__ __forceinline__ double2 kernelValue(KernelParams const &kp, double tx
   return make_double2(a.x + c.x, a.y + c.y);
 }
 
+// (accr, acci) += a x as four fused multiply-adds: written out, the compiler
+// forms a multiply, an FMA and an add per part (six instructions), and the
+// FP64 forms are bound by GB300's FP64 pipe
+__device__ __forceinline__ void cmacc(float &accr, float &acci, float2 a, float2 x) {
+  accr = fmaf(a.x, x.x, accr);
+  accr = fmaf(-a.y, x.y, accr);
+  acci = fmaf(a.x, x.y, acci);
+  acci = fmaf(a.y, x.x, acci);
+}
+__device__ __forceinline__ void cmacc(double &accr, double &acci, double2 a, double2 x) {
+  accr = fma(a.x, x.x, accr);
+  accr = fma(-a.y, x.y, accr);
+  acci = fma(a.x, x.y, acci);
+  acci = fma(a.y, x.x, acci);
+}
+
 __device__ __forceinline__ double warpSum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -395,10 +395,10 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
         } else {
           for (int r = lane; r < p; r += 32) {
             double2 x = Mem::ld(ci + r), y = Mem::ld(cj + r);
-            al += x.x * x.x + x.y * x.y;
-            be += y.x * y.x + y.y * y.y;
-            gr += x.x * y.x + x.y * y.y;     // conj(x) y
-            gi += x.x * y.y - x.y * y.x;
+            al = fma(x.x, x.x, fma(x.y, x.y, al));
+            be = fma(y.x, y.x, fma(y.y, y.y, be));
+            gr = fma(x.x, y.x, fma(x.y, y.y, gr));     // conj(x) y
+            gi = fma(x.x, y.y, fma(-x.y, y.x, gi));
           }
           al = warpSum(al);
           be = warpSum(be);
@@ -550,8 +550,8 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
       double yr = 0, yi = 0;
       for (int r = lane; r < p; r += 32) {
         double2 q = Mem::ldC(qa + r), z = myB[r];
-        yr += q.x * z.x + q.y * z.y;        // conj(q) z
-        yi += q.x * z.y - q.y * z.x;
+        yr = fma(q.x, z.x, fma(q.y, z.y, yr));        // conj(q) z
+        yi = fma(q.x, z.y, fma(-q.y, z.x, yi));
       }
       yr = warpSum(yr);
       yi = warpSum(yi);
@@ -564,8 +564,7 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
         double2 const y = myY[a];
         if (y.x == 0.0 && y.y == 0.0) continue;
         double2 const t = Mem::ldC(M + (int64_t)a * LD + i);
-        sr += t.x * y.x - t.y * y.y;
-        si += t.x * y.y + t.y * y.x;
+        cmacc(sr, si, t, y);
       }
       out[(int64_t)j * p + i] = make_double2(sr, si);
     }
@@ -595,8 +594,7 @@ __global__ void denseRowsKernel(PointsDev src, int64_t nSrc, PointsDev tgt,
                                useSrcN ? src.nx[j] : 0.0, useSrcN ? src.ny[j] : 0.0);
       for (int c = 0; c < rc; ++c) {
         double2 xv = x[j * ldx + r0 + c];
-        accr[c] += kv.x * xv.x - kv.y * xv.y;
-        acci[c] += kv.x * xv.y + kv.y * xv.x;
+        cmacc(accr[c], acci[c], kv, xv);
       }
     }
     for (int c = 0; c < rc; ++c) {
@@ -743,20 +741,15 @@ applyGemvKernel(ApplyItem const *__restrict__ items, ApplyContrib const *__restr
       }
       T2 const x0 = x[(j + 0 * S) * xs], x1 = x[(j + 1 * S) * xs];
       T2 const x2 = x[(j + 2 * S) * xs], x3 = x[(j + 3 * S) * xs];
-      accr += a0.x * x0.x - a0.y * x0.y;
-      acci += a0.x * x0.y + a0.y * x0.x;
-      accr += a1.x * x1.x - a1.y * x1.y;
-      acci += a1.x * x1.y + a1.y * x1.x;
-      accr += a2.x * x2.x - a2.y * x2.y;
-      acci += a2.x * x2.y + a2.y * x2.x;
-      accr += a3.x * x3.x - a3.y * x3.y;
-      acci += a3.x * x3.y + a3.y * x3.x;
+      cmacc(accr, acci, a0, x0);
+      cmacc(accr, acci, a1, x1);
+      cmacc(accr, acci, a2, x2);
+      cmacc(accr, acci, a3, x3);
     }
     for (; j < n; j += S) {
       T2 const a0 = active ? a[(int64_t)j * lda] : mk2<T2>(0, 0);
       T2 const x0 = x[j * xs];
-      accr += a0.x * x0.x - a0.y * x0.y;
-      acci += a0.x * x0.y + a0.y * x0.x;
+      cmacc(accr, acci, a0, x0);
     }
   }
   part[warp][lane] = mk2<T2>(accr, acci);
@@ -895,8 +888,7 @@ __global__ void __launch_bounds__(32 * NW, sizeof(T2) == 8 ? 8 : 4) applyPipeKer
       for (int u = 0; u < 4; ++u)
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          accr[4 * u + q] += a[u].x * x[q].x - a[u].y * x[q].y;
-          acci[4 * u + q] += a[u].x * x[q].y + a[u].y * x[q].x;
+          cmacc(accr[4 * u + q], acci[4 * u + q], a[u], x[q]);
         }
     }
     __syncthreads();
@@ -971,8 +963,7 @@ __global__ void __launch_bounds__(256) applyTileKernel(
 #pragma unroll
         for (int q = 0; q < PER; ++q) {
           T2 const b = Bs[kk][c0 + q * (NT / 32)];
-          accr[q] += a.x * b.x - a.y * b.y;
-          acci[q] += a.x * b.y + a.y * b.x;
+          cmacc(accr[q], acci[q], a, b);
         }
       }
       __syncthreads();

@@ -340,8 +340,8 @@ __global__ void __launch_bounds__(512) hqrKernel(HqrDesc const *__restrict__ des
       double sr = 0.0, si = 0.0;
       for (int i = k + 1 + lane; i < m; i += 32) {
         double2 const x = Mem::ld(col + i), a = Mem::ld(cj + i);
-        sr += x.x * a.x + x.y * a.y;
-        si += x.x * a.y - x.y * a.x;
+        sr = fma(x.x, a.x, fma(x.y, a.y, sr));
+        si = fma(x.x, a.y, fma(-x.y, a.x, si));
       }
       sr = warpSum(sr);
       si = warpSum(si);
@@ -403,8 +403,8 @@ __global__ void __launch_bounds__(512) hqrKernel(HqrDesc const *__restrict__ des
       double sr = 0.0, si = 0.0;
       for (int r = i + 1 + lane; r < m; r += 32) {
         double2 const x = Mem::ld(v + r), a = Mem::ld(qj + r);
-        sr += x.x * a.x + x.y * a.y;
-        si += x.x * a.y - x.y * a.x;
+        sr = fma(x.x, a.x, fma(x.y, a.y, sr));
+        si = fma(x.x, a.y, fma(-x.y, a.x, si));
       }
       sr = warpSum(sr);
       si = warpSum(si);
@@ -465,10 +465,10 @@ __global__ void __launch_bounds__(512) sketchJacobiKernel(JacobiDesc const *__re
         double al = 0, be = 0, gr = 0, gi = 0;
         for (int r = lane; r < rd; r += 32) {
           double2 const x = Mem::ld(ci + r), y = Mem::ld(cj + r);
-          al += x.x * x.x + x.y * x.y;
-          be += y.x * y.x + y.y * y.y;
-          gr += x.x * y.x + x.y * y.y;
-          gi += x.x * y.y - x.y * y.x;
+          al = fma(x.x, x.x, fma(x.y, x.y, al));
+          be = fma(y.x, y.x, fma(y.y, y.y, be));
+          gr = fma(x.x, y.x, fma(x.y, y.y, gr));
+          gi = fma(x.x, y.y, fma(-x.y, y.x, gi));
         }
         al = warpSum(al);
         be = warpSum(be);
