@@ -75,7 +75,8 @@ class _FacStatsC(ctypes.Structure):
         (n, ctypes.c_int64) for n in (
             "numSketched", "sketchRetries", "sketchFallbacks", "sketchMaxWidth")] + [
         (n, ctypes.c_double) for n in ("sketchMs", "sketchMeanWidth")] + [
-        ("applyBufferBytes", ctypes.c_int64), ("sketchPhaseMs", ctypes.c_double * 8)]
+        ("applyBufferBytes", ctypes.c_int64), ("sketchPhaseMs", ctypes.c_double * 8),
+        ("reexpSvds", ctypes.c_int64)]
 
 
 class _RngC(ctypes.Structure):

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -307,20 +308,31 @@ void factorize(bfgFac f) {
   // FIRST/MIDDLE blocks by where their Jacobi working set lives: shared
   // memory (8 or 16 warps), global memory with one CTA, or global memory
   // with a thread-block cluster for the largest ranks (the critical path)
-  std::vector<bfg::FillDesc> fill, reSmem8, reSmem16, reGlobal, reCluster;
+  // Blocks with the same Z_equiv (rank, equivalent circle, check circle,
+  // wavenumber) share one SVD: a group's leader carries the largest n of its
+  // members and is routed by it; every member gets its own Z_shift.
+  struct GroupList {
+    std::vector<bfg::FillDesc> lead;
+    std::vector<std::vector<bfg::FillDesc>> mem;
+  };
+  std::vector<bfg::FillDesc> fill, full;
+  GroupList reSmem8, reSmem16, reGlobal, reCluster;
   std::vector<bfg::SketchInput> sketch;
   int32_t maxProxyN = 1;
   int64_t maxRank = 0;
   bool const sketchCut = f->opts.pinvCut == 1 && f->opts.pinvTol >= kDfJacobiMinCut;
-  auto route = [&](bfg::FillDesc const &d) {
+  auto route = [&](bfg::FillDesc const &d, std::vector<bfg::FillDesc> &&members) {
+    GroupList *g;
     if (d.m <= 16 && bfg::reexpansionSmemBytes(d.m, d.n, 8) <= kSmemLimit)
-      reSmem8.push_back(d);
+      g = &reSmem8;
     else if (bfg::reexpansionSmemBytes(d.m, d.n, 16) <= kSmemLimit)
-      reSmem16.push_back(d);
+      g = &reSmem16;
     else if (d.m >= kClusterMinRank)
-      reCluster.push_back(d);
+      g = &reCluster;
     else
-      reGlobal.push_back(d);
+      g = &reGlobal;
+    g->lead.push_back(d);
+    g->mem.push_back(std::move(members));
   };
   for (auto const &b : plan.blocks) {
     bfg::FillDesc d = toDesc(b);
@@ -364,15 +376,8 @@ void factorize(bfgFac f) {
       sketch.push_back(bfg::SketchInput{d, l, 0});
       continue;
     }
-    route(d);
+    full.push_back(d);
   }
-  // largest Jacobi first, so that the longest CTAs start in the first wave
-  auto cost = [](bfg::FillDesc const &d) {
-    return (double)d.m * d.m * (3.0 * d.m + d.n);
-  };
-  auto byCost = [&](bfg::FillDesc const &a, bfg::FillDesc const &b) { return cost(a) > cost(b); };
-  for (auto *v : {&reSmem8, &reSmem16, &reGlobal, &reCluster})
-    std::stable_sort(v->begin(), v->end(), byCost);
   std::stable_sort(fill.begin(), fill.end(), [](bfg::FillDesc const &a, bfg::FillDesc const &b) {
     return (int64_t)a.m * a.n > (int64_t)b.m * b.n;
   });
@@ -404,7 +409,7 @@ void factorize(bfgFac f) {
                                  sketchCapture(f->opts), arena, kSketchBudgetEntries, s, &back,
                                  &rep),
        "randomized re-expansion");
-    for (auto const &d : back) route(d);
+    full.insert(full.end(), back.begin(), back.end());
     f->stats.numSketched = rep.blocks;
     f->stats.sketchRetries = rep.retries;
     f->stats.sketchFallbacks = rep.fallbacks;
@@ -416,6 +421,63 @@ void factorize(bfgFac f) {
   }
   ck(cudaEventRecord(eSketch, s), "event");
 
+  // the full path's groups, routed by their leaders
+  {
+    std::map<std::array<double, 8>, size_t> key;
+    std::vector<std::vector<bfg::FillDesc>> groups;
+    for (auto const &d : full) {
+      std::array<double, 8> const k8 = {(double)d.m, d.ceq[0], d.ceq[1], d.ceq[2],
+                                        d.cchk[0], d.cchk[1], d.cchk[2], d.k};
+      auto it = key.find(k8);
+      if (it == key.end()) {
+        key.emplace(k8, groups.size());
+        groups.push_back({d});
+      } else {
+        groups[it->second].push_back(d);
+      }
+    }
+    for (auto &g : groups) {
+      bfg::FillDesc lead = g[0];
+      for (auto const &m : g) lead.n = std::max(lead.n, m.n);
+      route(lead, std::move(g));
+    }
+    f->stats.reexpSvds = (int64_t)groups.size();
+  }
+  // largest work first, so that the longest CTAs start in the first wave
+  auto cost = [](bfg::FillDesc const &lead, std::vector<bfg::FillDesc> const &mem) {
+    double n = 0;
+    for (auto const &m : mem) n += m.n;
+    return (double)lead.m * lead.m * (3.0 * lead.m + n);
+  };
+  for (GroupList *g : {&reSmem8, &reSmem16, &reGlobal, &reCluster}) {
+    std::vector<size_t> order(g->lead.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+      return cost(g->lead[a], g->mem[a]) > cost(g->lead[b], g->mem[b]);
+    });
+    GroupList sorted;
+    for (size_t i : order) {
+      sorted.lead.push_back(g->lead[i]);
+      sorted.mem.push_back(std::move(g->mem[i]));
+    }
+    *g = std::move(sorted);
+  }
+  // a range of groups as the kernels take it: leaders, members back to back,
+  // group starts
+  auto flatten = [](GroupList const &g, size_t i0, size_t i1, std::vector<bfg::FillDesc> &lead,
+                    std::vector<bfg::FillDesc> &mem, std::vector<int32_t> &start) {
+    lead.assign(g.lead.begin() + (long)i0, g.lead.begin() + (long)i1);
+    mem.clear();
+    start.assign(1, 0);
+    for (size_t i = i0; i < i1; ++i) {
+      mem.insert(mem.end(), g.mem[i].begin(), g.mem[i].end());
+      start.push_back((int32_t)mem.size());
+    }
+  };
+  DevBuf dMem, dStart;
+  std::vector<bfg::FillDesc> leadV, memV;
+  std::vector<int32_t> startV;
+
   auto maxBytes = [](std::vector<bfg::FillDesc> const &v, int warps, bool geoOnly) {
     int64_t m = 0;
     for (auto const &d : v)
@@ -423,44 +485,56 @@ void factorize(bfgFac f) {
                               : bfg::reexpansionSmemBytes(d.m, d.n, warps));
     return (int32_t)m;
   };
-  upload(dSmem8, reSmem8, s, "descriptors");
-  ck(bfg::launchReexpansion(dSmem8.as<bfg::FillDesc>(), (int32_t)reSmem8.size(), src, kpProxy,
+  DevBuf dMem16, dStart16;
+  flatten(reSmem8, 0, reSmem8.lead.size(), leadV, memV, startV);
+  upload(dSmem8, leadV, s, "descriptors");
+  upload(dMem, memV, s, "descriptors");
+  upload(dStart, startV, s, "descriptors");
+  ck(bfg::launchReexpansion(dSmem8.as<bfg::FillDesc>(), (int32_t)leadV.size(), src, kpProxy,
                             f->opts.pinvCut, f->opts.pinvTol, arena, nullptr, nullptr, nullptr,
-                            st, 0, maxBytes(reSmem8, 8, false), 256, f->opts.jacobiArith, s),
+                            st, 0, maxBytes(leadV, 8, false), 256, f->opts.jacobiArith, s,
+                            dMem.as<bfg::FillDesc>(), dStart.as<int32_t>()),
      "re-expansion kernel");
-  upload(dSmem16, reSmem16, s, "descriptors");
-  ck(bfg::launchReexpansion(dSmem16.as<bfg::FillDesc>(), (int32_t)reSmem16.size(), src, kpProxy,
+  flatten(reSmem16, 0, reSmem16.lead.size(), leadV, memV, startV);
+  upload(dSmem16, leadV, s, "descriptors");
+  upload(dMem16, memV, s, "descriptors");
+  upload(dStart16, startV, s, "descriptors");
+  ck(bfg::launchReexpansion(dSmem16.as<bfg::FillDesc>(), (int32_t)leadV.size(), src, kpProxy,
                             f->opts.pinvCut, f->opts.pinvTol, arena, nullptr, nullptr, nullptr,
-                            st, 0, maxBytes(reSmem16, 16, false), 512, f->opts.jacobiArith, s),
+                            st, 0, maxBytes(leadV, 16, false), 512, f->opts.jacobiArith, s,
+                            dMem16.as<bfg::FillDesc>(), dStart16.as<int32_t>()),
      "re-expansion kernel");
   ck(cudaEventRecord(eSmem, s), "event");
 
   // global-memory working sets, in batches bounded by the scratch budget
   int32_t const clusterCtas = bfg::reexpansionClusterCtas();
   for (int mode = 1; mode <= 2; ++mode) {
-    std::vector<bfg::FillDesc> const &list = mode == 1 ? reGlobal : reCluster;
+    GroupList const &list = mode == 1 ? reGlobal : reCluster;
     int32_t const warps = mode == 1 ? 16 : 16 * clusterCtas;
     size_t i0 = 0;
-    while (i0 < list.size()) {
+    while (i0 < list.lead.size()) {
       std::vector<int64_t> offs;
       int64_t total = 0;
       size_t i1 = i0;
-      while (i1 < list.size()) {
-        int64_t e = bfg::reexpansionScratchEntries(list[i1].m, warps);
+      while (i1 < list.lead.size()) {
+        int64_t e = bfg::reexpansionScratchEntries(list.lead[i1].m, warps);
         if (i1 > i0 && total + e > kScratchBudgetEntries) break;
         offs.push_back(total);
         total += e;
         ++i1;
       }
-      std::vector<bfg::FillDesc> batch(list.begin() + (long)i0, list.begin() + (long)i1);
+      flatten(list, i0, i1, leadV, memV, startV);
       ck(scratch.ensure((size_t)total * sizeof(double2)), "re-expansion scratch");
-      ck(dFlags.ensure(batch.size() * clusterCtas * sizeof(int32_t)), "re-expansion flags");
-      upload(dBatch, batch, s, "descriptors");
+      ck(dFlags.ensure(leadV.size() * clusterCtas * sizeof(int32_t)), "re-expansion flags");
+      upload(dBatch, leadV, s, "descriptors");
       upload(dScratchOff, offs, s, "descriptors");
-      ck(bfg::launchReexpansion(dBatch.as<bfg::FillDesc>(), (int32_t)batch.size(), src, kpProxy,
+      upload(dMem, memV, s, "descriptors");
+      upload(dStart, startV, s, "descriptors");
+      ck(bfg::launchReexpansion(dBatch.as<bfg::FillDesc>(), (int32_t)leadV.size(), src, kpProxy,
                                 f->opts.pinvCut, f->opts.pinvTol, arena, scratch.as<double2>(),
                                 dScratchOff.as<int64_t>(), dFlags.as<int32_t>(), st, mode,
-                                maxBytes(batch, 0, true), 512, f->opts.jacobiArith, s),
+                                maxBytes(leadV, 0, true), 512, f->opts.jacobiArith, s,
+                                dMem.as<bfg::FillDesc>(), dStart.as<int32_t>()),
          mode == 1 ? "re-expansion kernel (global)" : "re-expansion kernel (cluster)");
       // the batch's descriptors, offsets and scratch are reused by the next
       ck(cudaStreamSynchronize(s), "re-expansion");

@@ -221,11 +221,17 @@ __device__ int reexpScaleExp(int eTop, int p, int32_t *clusterFlags, int rank) {
 // kDf: the Jacobi sweeps in double-float (~48 significant bits, FP32
 // arithmetic, about 6x fewer FP64 instructions; the rotation angles, the
 // singular values and the output stay FP64), else in FP64
+// Blocks with the same Z_equiv (the same rank, equivalent and check circles
+// and wavenumber) share one SVD: descriptor `blk` is a group's leader (its n
+// the largest over the group), and with `members` non-null the group's
+// blocks are members[groupStart[blk] .. groupStart[blk + 1]), each of which
+// gets its own Z_shift from the one pseudo-inverse.
 template <int kMode, bool kDf>
 __global__ void __launch_bounds__(512) reexpansionKernel(
     FillDesc const *__restrict__ descs, PointsDev src, KernelParams kp, int32_t cutMode,
     double cutTol, double2 *arena, double2 *scratch, int64_t const *scratchOff,
-    int32_t *flags, int32_t *status) {
+    int32_t *flags, int32_t *status, FillDesc const *__restrict__ members,
+    int32_t const *__restrict__ groupStart) {
   using Mem = ReexpMem<kMode, kDf>;
   extern __shared__ double2 smem2[];
   int const ctas = kMode == 2 ? kClusterCtas : 1;
@@ -274,25 +280,6 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
       eqY[a] = d.ceq[2] * s + d.ceq[1];
       eqNx[a] = c;
       eqNy[a] = s;
-    }
-    if (d.kind == kFirst) {
-      for (int b = tid; b < n; b += nthr) {
-        int64_t const sj = d.s0 + b;
-        orX[b] = src.x[sj];
-        orY[b] = src.y[sj];
-        orNx[b] = (useSrcN && src.nx) ? src.nx[sj] : 0.0;
-        orNy[b] = (useSrcN && src.ny) ? src.ny[sj] : 0.0;
-      }
-    } else {
-      double const scale2 = kTwoPiD / (double)n;
-      for (int b = tid; b < n; b += nthr) {
-        double s, c;
-        sincos(scale2 * b, &s, &c);
-        orX[b] = d.corig[2] * c + d.corig[0];
-        orY[b] = d.corig[2] * s + d.corig[1];
-        orNx[b] = c;
-        orNy[b] = s;
-      }
     }
   }
   __syncthreads();
@@ -532,9 +519,34 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
   }
   __syncthreads();
 
-  // x_j = T (w .* (Q^H z_j)); one warp per output column
-  double2 *out = arena + d.arenaOff;
-  for (int j = gWarp; j < n; j += gWarps) {
+  // every block of the group: its source points (Z_orig's columns), then
+  // x_j = T (w .* (Q^H z_j)), one warp per output column
+  int const g0 = members ? groupStart[blk] : 0, g1 = members ? groupStart[blk + 1] : 1;
+  for (int gm = g0; gm < g1; ++gm) {
+  FillDesc const dm = members ? members[gm] : d;
+  int const nm = dm.n;
+  if (dm.kind == kFirst) {
+    for (int b = tid; b < nm; b += nthr) {
+      int64_t const sj = dm.s0 + b;
+      orX[b] = src.x[sj];
+      orY[b] = src.y[sj];
+      orNx[b] = (useSrcN && src.nx) ? src.nx[sj] : 0.0;
+      orNy[b] = (useSrcN && src.ny) ? src.ny[sj] : 0.0;
+    }
+  } else {
+    double const scale2 = kTwoPiD / (double)nm;
+    for (int b = tid; b < nm; b += nthr) {
+      double s, c;
+      sincos(scale2 * b, &s, &c);
+      orX[b] = dm.corig[2] * c + dm.corig[0];
+      orY[b] = dm.corig[2] * s + dm.corig[1];
+      orNx[b] = c;
+      orNy[b] = s;
+    }
+  }
+  __syncthreads();
+  double2 *out = arena + dm.arenaOff;
+  for (int j = gWarp; j < nm; j += gWarps) {
     for (int r = lane; r < p; r += 32) {
       double2 z = kernelValue(kp, chkX[r], chkY[r], 0.0, 0.0, orX[j], orY[j], orNx[j], orNy[j]);
       myB[r] = z;
@@ -569,6 +581,8 @@ __global__ void __launch_bounds__(512) reexpansionKernel(
       out[(int64_t)j * p + i] = make_double2(sr, si);
     }
     __syncwarp();
+  }
+  __syncthreads();   // the next member's points overwrite these
   }
 }
 
@@ -1070,7 +1084,8 @@ cudaError_t launchReexpansionT(FillDesc const *descs, int32_t nDesc, PointsDev s
                                KernelParams kp, int32_t cutMode, double cutTol,
                                double2 *arena, double2 *scratch, int64_t const *scratchOff,
                                int32_t *flags, int32_t *status, int32_t mode,
-                               int32_t smemBytes, int32_t threads, cudaStream_t stream) {
+                               int32_t smemBytes, int32_t threads, cudaStream_t stream,
+                               FillDesc const *members, int32_t const *groupStart) {
   if (nDesc == 0) return cudaSuccess;
   cudaError_t e;
   if (mode == 0) {
@@ -1078,13 +1093,15 @@ cudaError_t launchReexpansionT(FillDesc const *descs, int32_t nDesc, PointsDev s
                              smemBytes);
     if (e != cudaSuccess) return e;
     reexpansionKernel<0, kDf><<<nDesc, threads, smemBytes, stream>>>(
-        descs, src, kp, cutMode, cutTol, arena, scratch, scratchOff, flags, status);
+        descs, src, kp, cutMode, cutTol, arena, scratch, scratchOff, flags, status, members,
+        groupStart);
   } else if (mode == 1) {
     e = cudaFuncSetAttribute(reexpansionKernel<1, kDf>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              smemBytes);
     if (e != cudaSuccess) return e;
     reexpansionKernel<1, kDf><<<nDesc, threads, smemBytes, stream>>>(
-        descs, src, kp, cutMode, cutTol, arena, scratch, scratchOff, flags, status);
+        descs, src, kp, cutMode, cutTol, arena, scratch, scratchOff, flags, status, members,
+        groupStart);
   } else {
     e = cudaFuncSetAttribute(reexpansionKernel<2, kDf>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              smemBytes);
@@ -1102,7 +1119,7 @@ cudaError_t launchReexpansionT(FillDesc const *descs, int32_t nDesc, PointsDev s
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     e = cudaLaunchKernelEx(&cfg, reexpansionKernel<2, kDf>, descs, src, kp, cutMode, cutTol,
-                           arena, scratch, scratchOff, flags, status);
+                           arena, scratch, scratchOff, flags, status, members, groupStart);
     if (e != cudaSuccess) return e;
   }
   return cudaGetLastError();
@@ -1113,12 +1130,15 @@ cudaError_t launchReexpansion(FillDesc const *descs, int32_t nDesc, PointsDev sr
                               double2 *arena, double2 *scratch, int64_t const *scratchOff,
                               int32_t *flags, int32_t *status, int32_t mode,
                               int32_t smemBytes, int32_t threads, int32_t doubleFloat,
-                              cudaStream_t stream) {
+                              cudaStream_t stream, FillDesc const *members,
+                              int32_t const *groupStart) {
   if (doubleFloat)
     return launchReexpansionT<true>(descs, nDesc, src, kp, cutMode, cutTol, arena, scratch,
-                                    scratchOff, flags, status, mode, smemBytes, threads, stream);
+                                    scratchOff, flags, status, mode, smemBytes, threads, stream,
+                                    members, groupStart);
   return launchReexpansionT<false>(descs, nDesc, src, kp, cutMode, cutTol, arena, scratch,
-                                   scratchOff, flags, status, mode, smemBytes, threads, stream);
+                                   scratchOff, flags, status, mode, smemBytes, threads, stream,
+                                   members, groupStart);
 }
 
 cudaError_t launchDenseRows(PointsDev src, int64_t nSrc, PointsDev tgt,

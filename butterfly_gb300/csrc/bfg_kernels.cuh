@@ -44,7 +44,9 @@ cudaError_t launchFillBlocks(FillDesc const *descs, int32_t nDesc, PointsDev src
                              int32_t maxProxyN, int32_t *status, cudaStream_t stream);
 
 // Fills FIRST/MIDDLE blocks: proxy kernel matrices + pseudo-inverse
-// re-expansion.  mode 0: working matrix in shared memory (smemBytes =
+// re-expansion.  With `members`, descriptor i leads a group of blocks with
+// the same Z_equiv (members[groupStart[i] .. groupStart[i + 1]), its n the
+// largest of theirs): one SVD, every member's Z_shift.  mode 0: working matrix in shared memory (smemBytes =
 // reexpansionSmemBytes); mode 1: in global `scratch` at scratchOff[block],
 // one CTA per block; mode 2: in global scratch, one thread-block cluster of
 // reexpansionClusterCtas() CTAs per block, `flags` holding one int per CTA.
@@ -54,7 +56,8 @@ cudaError_t launchReexpansion(FillDesc const *descs, int32_t nDesc, PointsDev sr
                               double2 *arena, double2 *scratch, int64_t const *scratchOff,
                               int32_t *flags, int32_t *status, int32_t mode,
                               int32_t smemBytes, int32_t threads, int32_t doubleFloat,
-                              cudaStream_t stream);
+                              cudaStream_t stream, FillDesc const *members = nullptr,
+                              int32_t const *groupStart = nullptr);
 
 int64_t reexpansionSmemBytes(int32_t m, int32_t n, int32_t warps);
 int64_t reexpansionGeoBytes(int32_t m, int32_t n);

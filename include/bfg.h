@@ -136,6 +136,8 @@ typedef struct bfgFacStats {
   double sketchPhaseMs[8];    /* randomized path by phase: fills, Z Omega,
                                  qr(Y), Z^H Q, qr(G), Jacobi, weights and
                                  capture test, output products */
+  int64_t reexpSvds;          /* SVDs of the full path: its blocks with the
+                                 same Z_equiv share one */
 } bfgFacStats;
 
 /* Contexts: one CUDA device and one stream; calls on a context are
