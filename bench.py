@@ -854,6 +854,7 @@ def fac_summary(fac, wall_s):
             "sketched_blocks": st["numSketched"], "sketch_ms": st["sketchMs"],
             "sketch_mean_width": st["sketchMeanWidth"], "sketch_max_width": st["sketchMaxWidth"],
             "sketch_retries": st["sketchRetries"], "reexp_svds": st["reexpSvds"],
+            "sketch_svds": st["sketchGroups"],
             "sketch_phase_ms": dict(zip(("fill", "z_omega", "qr_y", "zh_q", "qr_g", "jacobi",
                                          "weights", "output"), st["sketchPhaseMs"])),
             "fill_ms": st["fillMs"],

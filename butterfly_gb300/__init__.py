@@ -76,7 +76,7 @@ class _FacStatsC(ctypes.Structure):
             "numSketched", "sketchRetries", "sketchFallbacks", "sketchMaxWidth")] + [
         (n, ctypes.c_double) for n in ("sketchMs", "sketchMeanWidth")] + [
         ("applyBufferBytes", ctypes.c_int64), ("sketchPhaseMs", ctypes.c_double * 8),
-        ("reexpSvds", ctypes.c_int64)]
+        ("reexpSvds", ctypes.c_int64), ("sketchGroups", ctypes.c_int64)]
 
 
 class _RngC(ctypes.Structure):

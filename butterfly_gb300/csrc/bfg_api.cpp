@@ -411,6 +411,7 @@ void factorize(bfgFac f) {
        "randomized re-expansion");
     full.insert(full.end(), back.begin(), back.end());
     f->stats.numSketched = rep.blocks;
+    f->stats.sketchGroups = rep.groups;
     f->stats.sketchRetries = rep.retries;
     f->stats.sketchFallbacks = rep.fallbacks;
     f->stats.sketchMaxWidth = rep.maxWidth;

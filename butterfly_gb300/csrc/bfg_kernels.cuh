@@ -76,6 +76,7 @@ struct SketchInput {
 };
 struct SketchReport {
   int64_t blocks = 0;      // blocks computed by this path
+  int64_t groups = 0;      // their distinct Z_equiv (one sketch and SVD each)
   int64_t retries = 0;     // sketches redone with a wider l
   int64_t fallbacks = 0;   // blocks handed back to the full path
   int64_t maxWidth = 0, sumWidth = 0;

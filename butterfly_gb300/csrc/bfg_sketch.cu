@@ -35,6 +35,8 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <array>
+#include <map>
 #include <cmath>
 #include <cstdint>
 #include <vector>
@@ -588,9 +590,6 @@ uint64_t splitmixHost(uint64_t x) {
   return x ^ (x >> 31);
 }
 
-int64_t scratchEntries(int64_t p, int64_t n, int64_t l) {
-  return p * p + 3 * p * l + 2 * l * l + p * n + 2 * l * n + l + l + 4;
-}
 
 // modes of the HQR / Jacobi launches: a whole cluster for large blocks
 bool hqrCluster(int64_t p, int64_t l) { return p * l >= (int64_t)1 << 17; }
@@ -720,11 +719,39 @@ cudaError_t runSketchReexpansion(std::vector<SketchInput> const &in, PointsDev s
     if ((err = cudaEventCreate(&x)) != cudaSuccess) return err;
   auto mark = [&](int i) { cudaEventRecord(pev.e[i], s); };
 
-  std::vector<SketchInput> queue = in;
-  // largest first, so that the longest blocks start in the first wave
-  auto cost = [](SketchInput const &a) { return (double)a.d.m * a.l * (a.l + a.d.m + a.d.n); };
+  // blocks with the same Z_equiv (rank, equivalent and check circles,
+  // wavenumber) form one group: one sketch, QR and SVD; every member its own
+  // Z_orig and Z_shift
+  struct Group {
+    std::vector<FillDesc> mem;
+    int32_t l, fullOk;
+  };
+  std::vector<Group> queue;
+  {
+    std::map<std::array<double, 8>, size_t> key;
+    for (SketchInput const &x : in) {
+      std::array<double, 8> const k8 = {(double)x.d.m, x.d.ceq[0], x.d.ceq[1], x.d.ceq[2],
+                                        x.d.cchk[0], x.d.cchk[1], x.d.cchk[2], x.d.k};
+      auto it = key.find(k8);
+      if (it == key.end()) {
+        key.emplace(k8, queue.size());
+        queue.push_back(Group{{x.d}, x.l, x.fullOk});
+      } else {
+        Group &g = queue[it->second];
+        g.mem.push_back(x.d);
+        g.l = std::max(g.l, x.l);
+        g.fullOk = g.fullOk && x.fullOk;
+      }
+    }
+  }
+  // largest first, so that the longest groups start in the first wave
+  auto cost = [](Group const &g) {
+    double n = 0;
+    for (auto const &d : g.mem) n += d.n;
+    return (double)g.mem[0].m * g.l * (g.l + g.mem[0].m) + (double)g.l * g.mem[0].m * n;
+  };
   std::stable_sort(queue.begin(), queue.end(),
-                   [&](SketchInput const &a, SketchInput const &b) { return cost(a) > cost(b); });
+                   [&](Group const &a, Group const &b) { return cost(a) > cost(b); });
   Buf scratch, dBlk, dTiles, dDesc, dHqr1, dHqr2, dJac1, dJac2, dW, dFail, dStatus;
   err = dStatus.ensure(sizeof(int32_t));
   if (err != cudaSuccess) return err;
@@ -735,41 +762,57 @@ cudaError_t runSketchReexpansion(std::vector<SketchInput> const &in, PointsDev s
 
   size_t q0 = 0;
   while (q0 < queue.size()) {
-    // a batch within the scratch budget (at least one block)
-    std::vector<SketchDev> blks;
+    // a batch of groups within the scratch budget (at least one): descs
+    // holds the groups' leaders (the sketch, QRs and SVD), then their
+    // members (Z_orig and the output products), memberOf[i] the leader of
+    // member nb + i
+    std::vector<SketchDev> blks, mems;
+    std::vector<size_t> memberOf;
     int64_t total = 0;
     size_t q1 = q0;
     while (q1 < queue.size()) {
-      SketchInput const &in1 = queue[q1];
-      int64_t const e = scratchEntries(in1.d.m, in1.d.n, in1.l);
+      Group const &gr = queue[q1];
+      int64_t const p = gr.mem[0].m, l = gr.l;
+      int64_t e = p * p + 3 * p * l + 2 * l * l + l + l + 4;
+      for (auto const &d : gr.mem) e += p * d.n + 2 * l * d.n;
       if (q1 > q0 && total + e > budgetEntries) break;
+      FillDesc const &d0 = gr.mem[0];
       SketchDev b{};
-      b.kind = in1.d.kind;
-      b.p = in1.d.m;
-      b.n = in1.d.n;
-      b.l = in1.l;
-      b.arenaOff = in1.d.arenaOff;
-      b.s0 = in1.d.s0;
+      b.kind = d0.kind;
+      b.p = d0.m;
+      b.n = d0.n;
+      b.l = gr.l;
+      b.arenaOff = d0.arenaOff;
+      b.s0 = d0.s0;
       for (int c = 0; c < 3; ++c) {
-        b.corig[c] = in1.d.corig[c];
-        b.ceq[c] = in1.d.ceq[c];
-        b.cchk[c] = in1.d.cchk[c];
+        b.corig[c] = d0.corig[c];
+        b.ceq[c] = d0.ceq[c];
+        b.cchk[c] = d0.cchk[c];
       }
-      b.k = in1.d.k;
+      b.k = d0.k;
       b.seed = splitmixHost(seedCounter++);
-      int64_t const p = b.p, n = b.n, l = b.l;
       int64_t o = total;
       b.oZ = o; o += p * p;
       b.oB0 = o; o += p * l;
       b.oB1 = o; o += p * l;
       b.oB2 = o; o += p * l;
       b.oM = o; o += 2 * l * l;
-      b.oZo = o; o += p * n;
-      b.oC = o; o += l * n;
-      b.oD = o; o += l * n;
       b.oTau = o; o += l;
       b.oSW = o; o += l;
       b.oFlags = o; o += 4;
+      for (auto const &d : gr.mem) {
+        SketchDev m = b;
+        m.kind = d.kind;
+        m.n = d.n;
+        m.arenaOff = d.arenaOff;
+        m.s0 = d.s0;
+        for (int c = 0; c < 3; ++c) m.corig[c] = d.corig[c];
+        m.oZo = o; o += p * d.n;
+        m.oC = o; o += l * d.n;
+        m.oD = o; o += l * d.n;
+        mems.push_back(m);
+        memberOf.push_back(blks.size());
+      }
       total = o;
       blks.push_back(b);
       ++q1;
@@ -778,24 +821,29 @@ cudaError_t runSketchReexpansion(std::vector<SketchInput> const &in, PointsDev s
     if (err != cudaSuccess) return err;
     double2 *S = static_cast<double2 *>(scratch.p);
     size_t const nb = blks.size();
+    std::vector<SketchDev> descs = blks;
+    descs.insert(descs.end(), mems.begin(), mems.end());
 
-    // fill
+    // fill: Z_equiv and Omega per group, Z_orig per member
     mark(0);
     std::vector<FillTileDesc> tiles;
+    auto addTiles = [&](size_t di, int w, int64_t cnt) {
+      for (int64_t e0 = 0; e0 < cnt; e0 += kFillTile) {
+        FillTileDesc t{};
+        t.blk = (int32_t)di;
+        t.what = w;
+        t.e0 = e0;
+        t.cnt = (int32_t)std::min<int64_t>(kFillTile, cnt - e0);
+        tiles.push_back(t);
+      }
+    };
     for (size_t i = 0; i < nb; ++i) {
-      SketchDev const &b = blks[i];
-      int64_t const cnts[3] = {(int64_t)b.p * b.p, (int64_t)b.p * b.l, (int64_t)b.p * b.n};
-      for (int w = 0; w < 3; ++w)
-        for (int64_t e0 = 0; e0 < cnts[w]; e0 += kFillTile) {
-          FillTileDesc t{};
-          t.blk = (int32_t)i;
-          t.what = w;
-          t.e0 = e0;
-          t.cnt = (int32_t)std::min<int64_t>(kFillTile, cnts[w] - e0);
-          tiles.push_back(t);
-        }
+      addTiles(i, 0, (int64_t)blks[i].p * blks[i].p);
+      addTiles(i, 1, (int64_t)blks[i].p * blks[i].l);
     }
-    if ((err = put(dBlk, blks, s)) != cudaSuccess) return err;
+    for (size_t i = 0; i < mems.size(); ++i)
+      addTiles(nb + i, 2, (int64_t)mems[i].p * mems[i].n);
+    if ((err = put(dBlk, descs, s)) != cudaSuccess) return err;
     if ((err = put(dTiles, tiles, s)) != cudaSuccess) return err;
     for (size_t t0 = 0; t0 < tiles.size(); t0 += ((size_t)1 << 30)) {
       size_t const cnt = std::min<size_t>((size_t)1 << 30, tiles.size() - t0);
@@ -870,32 +918,39 @@ cudaError_t runSketchReexpansion(std::vector<SketchInput> const &in, PointsDev s
       return err;
     if ((err = cudaStreamSynchronize(s)) != cudaSuccess) return err;
 
-    // accepted blocks: X = Q2 (W (diag(w) (T^H (Q^H Z_orig))))
+    // accepted groups: X = Q2 (W (diag(w) (T^H (Q^H Z_orig)))) per member
     std::vector<GemmDesc> gc, gd, ge, gx;
-    std::vector<SketchInput> requeue;
+    std::vector<Group> requeue;
     for (size_t i = 0; i < nb; ++i) {
       SketchDev const &b = blks[i];
-      SketchInput const &src1 = queue[q0 + i];
+      Group const &gr = queue[q0 + i];
       bool const full = b.l >= b.p;
       if (failed[i] && !full) {
-        SketchInput r = src1;
+        Group r = gr;
         r.l = std::min<int32_t>(b.p, 2 * b.l);
-        ++rep->retries;
+        rep->retries += (int64_t)gr.mem.size();
         if (r.fullOk && r.l > (int32_t)(0.8 * b.p)) {
-          fallback->push_back(r.d);
-          ++rep->fallbacks;
+          fallback->insert(fallback->end(), r.mem.begin(), r.mem.end());
+          rep->fallbacks += (int64_t)gr.mem.size();
         } else {
           requeue.push_back(r);
         }
         continue;
       }
+      rep->groups += 1;
+    }
+    for (size_t mi = 0; mi < mems.size(); ++mi) {
+      size_t const i = memberOf[mi];
+      SketchDev const &b = blks[i];
+      if (failed[i] && b.l < b.p) continue;
+      SketchDev const &m = mems[mi];
       double const *w = reinterpret_cast<double const *>(S + b.oSW) + b.l;
-      gc.push_back(GemmDesc{S + b.oB0, S + b.oZo, S + b.oC, nullptr, b.p, b.p, b.l, b.l, b.n, b.p, 1});
-      gd.push_back(GemmDesc{S + b.oM, S + b.oC, S + b.oD, w, 2 * b.l, b.l, b.l, b.l, b.n, b.l, 1});
-      ge.push_back(GemmDesc{S + b.oM + b.l, S + b.oD, S + b.oC, nullptr, 2 * b.l, b.l, b.l, b.l, b.n,
-                            b.l, 0});
-      gx.push_back(GemmDesc{S + b.oB2, S + b.oC, arena + b.arenaOff, nullptr, b.p, b.l, b.p, b.p, b.n,
-                            b.l, 0});
+      gc.push_back(GemmDesc{S + b.oB0, S + m.oZo, S + m.oC, nullptr, b.p, b.p, b.l, b.l, m.n, b.p, 1});
+      gd.push_back(GemmDesc{S + b.oM, S + m.oC, S + m.oD, w, 2 * b.l, b.l, b.l, b.l, m.n, b.l, 1});
+      ge.push_back(GemmDesc{S + b.oM + b.l, S + m.oD, S + m.oC, nullptr, 2 * b.l, b.l, b.l, b.l,
+                            m.n, b.l, 0});
+      gx.push_back(GemmDesc{S + b.oB2, S + m.oC, arena + m.arenaOff, nullptr, b.p, b.l, b.p, b.p,
+                            m.n, b.l, 0});
       ++rep->blocks;
       rep->maxWidth = std::max<int64_t>(rep->maxWidth, b.l);
       rep->sumWidth += b.l;

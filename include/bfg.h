@@ -138,6 +138,8 @@ typedef struct bfgFacStats {
                                  capture test, output products */
   int64_t reexpSvds;          /* SVDs of the full path: its blocks with the
                                  same Z_equiv share one */
+  int64_t sketchGroups;       /* SVDs of the randomized path, shared the same
+                                 way */
 } bfgFacStats;
 
 /* Contexts: one CUDA device and one stream; calls on a context are
