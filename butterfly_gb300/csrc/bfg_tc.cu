@@ -117,6 +117,9 @@ __device__ __forceinline__ uint64_t globalTimerNs() {
 // launch's wait limit, kWaitLimitNs unless a test lowers it) or as soon as
 // another role of the CTA has given up (*abort set)
 __device__ bool mbarWait(uint32_t bar, uint32_t parity, int volatile *abort, uint64_t limitNs) {
+  // a zero limit (the test hook) gives up at once, as a wait on a phase that
+  // never completes gives up once the limit has passed
+  if (limitNs == 0) return false;
   if (mbarTryWait(bar, parity)) return true;
   uint64_t const t0 = globalTimerNs();
   for (;;) {
@@ -329,9 +332,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
   tcFenceAfter();
   uint32_t const tmem = *tmemSlot;
 
+  // what each role has in flight, for the drains after an abort: the
+  // producer's issued bulk copies, each MMA thread's last committed chunk
+  int64_t issued = 0, lastMma = -1;
   if (warp == kProducerWarp) {
     // ---- bulk copies of the A planes and of the input rows (lane 0) ----
-    int64_t issued = 0;
     // descriptors are read one chunk ahead, off the wait-issue path
     TcChunk const *cp = ch;
     int64_t off = cp->tileOff, inRow = cp->inRow;
@@ -379,18 +384,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
       nc = ncN;
       inIsX = inIsXN;
     }
-    if (lane == 0 && *abortFlag)   // copies still in flight land before the CTA exits
-      for (int64_t j = issued > S ? issued - S : 0; j < issued; ++j) {
-        mbarDrain(fullX + 8 * (j % S), (uint32_t)((j / S) & 1));
-        mbarDrain(fullA + 8 * (j % S), (uint32_t)((j / S) & 1));
-      }
   } else if (warp == kMmaWarp || warp == kMmaWarp + 1) {
     // ---- MMAs: warp kMmaWarp issues the even chunks, the next warp the odd
     // ones, so one thread's waits and bookkeeping overlap the other's MMAs in
     // the tensor pipe; chunk i uses TMEM buffer i % 2, i.e. its thread's own ----
     int const parity = warp - kMmaWarp;
     if (lane == 0 && parity < nCh) {
-      int64_t last = -1;
+
       int32_t kg = ch[parity].kg, mg = ch[parity].mg;
       for (int64_t i = parity; i < nCh; i += 2) {
         int const s = (int)(i % S), b = (int)(i & 1);
@@ -433,12 +433,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
         }
         tcCommit(empty + 8 * s);
         tcCommit(accFull + 8 * b);
-        last = i;
+        lastMma = i;
         kg = kgN;
         mg = mgN;
       }
-      if (*abortFlag && last >= 0)
-        mbarDrain(empty + 8 * (last % S), (uint32_t)((last / S) & 1));
     }
   } else {
     struct Cd {            // builders: inputs of a chunk
@@ -624,6 +622,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
     }
   }
 
+  // After an abort, whatever a role still has in flight lands before the CTA
+  // frees its tensor memory and shared memory.  The drains come after a
+  // barrier: a role that finished its loop may have read the abort flag
+  // before another role gave up, and its copies or MMAs could then still be
+  // outstanding.  The flag is final here, the same for every thread.
+  tcFenceBefore();
+  __syncthreads();
+  if (*abortFlag) {
+    if (warp == kProducerWarp && lane == 0)
+      for (int64_t j = issued > S ? issued - S : 0; j < issued; ++j) {
+        mbarDrain(fullX + 8 * (j % S), (uint32_t)((j / S) & 1));
+        mbarDrain(fullA + 8 * (j % S), (uint32_t)((j / S) & 1));
+      }
+    if ((warp == kMmaWarp || warp == kMmaWarp + 1) && lane == 0 && lastMma >= 0)
+      mbarDrain(empty + 8 * (lastMma % S), (uint32_t)((lastMma / S) & 1));
+  }
   tcFenceBefore();
   __syncthreads();
   if (warp == kMmaWarp) {
