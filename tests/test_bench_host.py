@@ -75,3 +75,29 @@ def test_batched_reference_arm_is_unavailable():
     assert r.returncode == 0, r.stderr
     line = json.loads(r.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["unavailable"]
+
+
+def test_cpu_factorization_worker_times_the_oracle_factorization():
+    """The CPU factorization leg (child processes on the host cores): the
+    oracle's factorization of the 4,096-point workload in full."""
+    r = bench.cpu_factorization_worker("c1", 0)
+    assert r["full"] is True and r["seconds"] > 0 and r["blocks"] > 100
+
+
+def test_standin_port_over_a_plan_with_wrapped_values():
+    """The reference's apply algorithm over a plan's structure with stand-in
+    values in a buffer shorter than the plan: every block reads m n entries
+    of it, and the product of constant blocks is the analytic one."""
+    from oracle import bf_oracle as O
+    src = O.uniform_square_points(2048, 0)
+    tgt = O.curve_points("circle", 2048)
+    fac = O.Factorization(O.Helm2(40.0), src, tgt, leaf_size=64, eps=1e-8, fill=False)
+    text = fac.plan_text()
+    entries = O.parse_plan_entries(text)
+    assert entries == fac.num_entries()
+    big = max(b.m * b.n for b in fac.blocks())
+    data = np.full(big + 17, 1e-3 + 0j, dtype=np.complex128)
+    port = O.ApplyPort.from_plan(text, data, True, wrap=True)
+    full = O.ApplyPort.from_plan(text, np.full(entries, 1e-3 + 0j), True)
+    X = O.RefRng(2).complex_randn(2048 * 2).reshape(2048, 2)
+    assert np.allclose(port(X, 2), full(X, 2), rtol=1e-13, atol=0)
