@@ -131,6 +131,7 @@ def lib() -> ctypes.CDLL:
         "bfgBessel01": [_VP, _VP, _I64, _VP],
         "bfgMeasureFp64Rate": [_VP, ctypes.POINTER(ctypes.c_double)],
         "bfgFacSetTcWaitLimit": [_VP, ctypes.c_uint64],
+        "bfgFacSynchronize": [_VP],
         "bfgPlanHelm2": [ctypes.c_double, _VP, _I64, _VP, _I64, ctypes.POINTER(_FacOptionsC),
                          _VP, _VP, ctypes.c_char_p, _I64, ctypes.POINTER(_I64)],
         "bfgBessel01Host": [_VP, _I64, _VP],
@@ -500,6 +501,12 @@ class Fac:
                                               R, _VP(y_ptr), ldy, flags, _ptr(ms), cap,
                                               ctypes.byref(n)), "apply_timed")
         return ms[:n.value].copy()
+
+    def synchronize(self):
+        """Waits for the context's stream and raises BfgError(33,
+        BFG_ERROR_TIMEOUT) if an asynchronous tensor-core apply gave up on a
+        bounded wait (bfgFacSynchronize)."""
+        self.ctx.check(lib().bfgFacSynchronize(self.handle), "synchronize")
 
     def launch_info(self, original_order: bool = False) -> np.ndarray:
         """(entries, rows_in, rows_out) per launch of one apply."""

@@ -1395,6 +1395,15 @@ bfgStatus bfgFacCopyBlocks(bfgFac f, double *entries, int64_t capEntries, int64_
   });
 }
 
+bfgStatus bfgFacSynchronize(bfgFac f) {
+  if (!f) return BFG_ERROR_INVALID_ARGUMENTS;
+  return guarded(f->ctx, [&]() -> bfgStatus {
+    ck(cudaStreamSynchronize(f->ctx->stream), "synchronize");
+    checkTcStatus(f);
+    return BFG_OK;
+  });
+}
+
 bfgStatus bfgFacApply(bfgFac f, bfgPrecision prec, void const *X, int64_t ldx, int64_t R,
                       void *Y, int64_t ldy, uint32_t flags) {
   if (!f) return BFG_ERROR_INVALID_ARGUMENTS;

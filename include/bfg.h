@@ -238,6 +238,15 @@ bfgStatus bfgFacSetTcWaitLimit(bfgFac fac, uint64_t waitLimitNs);
 bfgStatus bfgFacAutotune(bfgFac fac, bfgPrecision precision, int64_t numRhs, double *stageMs,
                          int32_t capacity, int32_t *numStages);
 
+/* Waits for the context's stream and reports what the tensor-core applies
+ * enqueued since the last check left in their status word:
+ * BFG_ERROR_TIMEOUT when a bounded device wait ran out (the factorization
+ * stays usable).  The synchronising calls (bfgFacApplyHost,
+ * bfgFacApplyTimed, bfgFacAutotune) check it themselves; after
+ * asynchronous bfgFacApply calls, this is the check.  No counterpart in the
+ * reference (whose applies are synchronous host code). */
+bfgStatus bfgFacSynchronize(bfgFac fac);
+
 /* Y = A X -- bfMatMul (mat.c:183-185) with A the factorization.  X (numCols
  * x numRhs) and Y (numRows x numRhs) are DEVICE pointers: complex128 for
  * FP64, complex64 for FP32, BF16X2 and BF16X3.  The first apply in a
