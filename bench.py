@@ -118,6 +118,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-c2", action="store_true",
                     help="skip the 65,536-point workload's block (1 and 16 RHS)")
+    ap.add_argument("--no-c3", action="store_true",
+                    help="skip the 256-problem batched workload's block")
     ap.add_argument("--no-cpu-factorization", action="store_true",
                     help="skip the oracle factorization timings on the host cores")
     ap.add_argument("--profile", default="", choices=["", "fp64", "df64", "fp32", "bf16x3", "bf16x2"],
@@ -300,6 +302,14 @@ def run_batched(args, cfg):
     world, rank, local, dist = dist_setup()
     torch.cuda.set_device(local)
     ctx = B.Context(local)
+    line = batched_line(args, cfg, B, ctx, world, rank, local, dist)
+    if line is not None:
+        print(json.dumps(line))
+
+
+def batched_line(args, cfg, B, ctx, world, rank, local, dist):
+    """The batched workload's measurement as a dict (None off rank 0)."""
+    import torch
     sizes, problems, ks = batched_problems(B, cfg)
     t0 = time.perf_counter()
     # every problem's two quadtrees in one GPU pass (the same trees as the
@@ -374,7 +384,8 @@ def run_batched(args, cfg):
                                       B._VP(Yp.data_ptr()), R, 0))
     e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
     if rank != 0:
-        return
+        fac.close()
+        return None
     st = fac.stats()
     line = {"metric": METRIC, "value": rhs_s[head], "unit": "RHS/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
@@ -409,7 +420,8 @@ def run_batched(args, cfg):
                     "h2d_bytes_per_step": n * R * 16, "d2h_bytes_per_step": n * R * 16,
                     "precision": head},
             "clocks": clk, "gpu_launches": len(info) * args.steps}
-    print(json.dumps(line))
+    fac.close()
+    return line
 
 
 # ---------------------------------------------------------------------------
@@ -1140,6 +1152,15 @@ def main():
             c2 = secondary_c2(B, ctx, stream, args, dist)
         except Exception as exc:
             c2 = {"error": str(exc)[:200]}
+    c3 = None
+    if world == 1 and not args.no_c3:
+        try:
+            c3 = batched_line(args, CONFIGS["c3"], B, ctx, world, rank, local, dist)
+            c3 = {k: v for k, v in c3.items() if k not in ("metric", "n_gpus", "steps", "warmup",
+                                                           "higher_is_better", "scaling",
+                                                           "vs_baseline", "data")}
+        except Exception as exc:
+            c3 = {"error": str(exc)[:200]}
     cpu_fac = None
     if world == 1 and not args.no_cpu_factorization:
         cpu_fac = cpu_factorization([("c1", 0), ("c2", 10.0)])
@@ -1175,7 +1196,7 @@ def main():
             "factorization": fac_info, "rhs1": rhs1,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
             "gpu_launches": launches, "gmres": gm, "autotune": tuned,
-            "cpu_factorization": cpu_fac, "c2": c2,
+            "cpu_factorization": cpu_fac, "c2": c2, "c3": c3,
             "fp64_measured_tflops": FP64_MEASURED["tflops"]}
     print(json.dumps(line))
 
