@@ -129,9 +129,9 @@ def parse():
     ap.add_argument("--cpu-fac-budget", type=float, default=0.0, help=argparse.SUPPRESS)
     ap.add_argument("--no-gmres", action="store_true",
                     help="skip the multiple-scattering GMRES time-to-1e-8 measurement")
-    ap.add_argument("--learned", action="store_true",
-                    help="also train the learned preconditioner on GMRES solves of other "
-                         "scatterer layouts and compare it with block-Jacobi (about a minute)")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the learned preconditioner: training on GMRES solves of other "
+                         "scatterer layouts and FGMRES beside block-Jacobi (about a minute)")
     return ap.parse_args()
 
 
@@ -1176,7 +1176,7 @@ def main():
             gm = gmres_scattering(B, ctx)
         except Exception as exc:       # reported, the apply line still stands
             gm = {"error": str(exc)[:200]}
-        if args.learned:
+        if not args.no_learned and "error" not in gm:
             try:
                 gm["learned"] = learned_scattering(B, ctx)
             except Exception as exc:
