@@ -764,9 +764,10 @@ void checkTcStatus(bfgFac f) {
 }
 
 // chunk streams for R right-hand sides: the resident CTAs shared out over
-// the ceil(R / 16) tiles of every stream
+// the RHS tiles of every stream
 int32_t tcStreams(bfgFac_s::Tc const &tc, int64_t R) {
-  int64_t const tiles = (R + bfg::kTcRhsTile - 1) / bfg::kTcRhsTile;
+  int64_t const rt = bfg::tcRhsTile(R);
+  int64_t const tiles = (R + rt - 1) / rt;
   return (int32_t)std::max<int64_t>(1, tc.ctas / std::max<int64_t>(1, tiles));
 }
 

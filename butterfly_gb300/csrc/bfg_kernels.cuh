@@ -151,16 +151,15 @@ cudaError_t launchApplyReduce(int32_t const *rowSeg, int64_t const *segStart,
                               cudaStream_t stream);
 
 // Split-BF16 tensor-core apply (terms = 2 or 3 bf16 planes).
-int32_t tcSmemBytes(int32_t terms);
-// sets the kernel's shared-memory limit; returns resident CTAs per SM
+// sets the kernels' shared-memory limit; returns resident CTAs per SM
 cudaError_t tcPrepare(int32_t terms, int32_t *ctasPerSm);
 cudaError_t launchTcFill(int32_t terms, TcFill const *fills, int64_t nFills,
                          double2 const *arena64, uint8_t *tarena, cudaStream_t stream);
-// one stage: `ctas` chunk streams times ceil(R / 16) RHS tiles, one
-// persistent CTA each, the tiles of a stream adjacent in the grid; stream c
-// runs chunks [ctaChunk0[c], ctaChunk0[c+1]); status bit 4 = a bounded wait
-// expired
-constexpr int32_t kTcRhsTile = 16;
+// one stage: `ctas` chunk streams times ceil(R / tcRhsTile(R)) RHS tiles,
+// one persistent CTA each, the tiles of a stream adjacent in the grid;
+// stream c runs chunks [ctaChunk0[c], ctaChunk0[c+1]); status bit 4 = a
+// bounded wait expired.  The tile is 16 RHS for R <= 16, else 32.
+int32_t tcRhsTile(int64_t R);
 // every mbarrier wait of the kernel gives up after waitLimitNs (then the CTA
 // drains what it has in flight, frees its tensor memory and sets status bit 4)
 constexpr uint64_t kTcWaitLimitNs = 1000000000ull;

@@ -198,9 +198,10 @@ void makeApplyProgram(Plan const &plan, ApplyProgram &prog, int itemRows = kItem
 // stored as a pre-tiled bf16 A tile in the tensor arena.
 // ---------------------------------------------------------------------------
 constexpr int kTcRows = 128;          // MMA M: rows per item
-constexpr int kTcChunkCols = 64;      // most complex columns per chunk (8 MMA k-steps)
+constexpr int kTcChunkCols = 32;      // most complex columns per chunk (4 MMA k-steps)
 // k-groups (4 complex columns) per chunk for an item of mg row groups: an A
-// plane holds at most 64 cores (8 KB), the count is even (whole k-steps)
+// plane holds at most 64 cores (8 KB) and the B planes of a 32-RHS tile at
+// most 8 k-groups; the count is even (whole k-steps)
 inline int32_t tcMaxKGroups(int32_t mg) {
   int32_t k = 64 / (mg < 1 ? 1 : mg);
   if (k > kTcChunkCols / 4) k = kTcChunkCols / 4;

@@ -6,16 +6,18 @@
 // each right-hand side is split the same way as it is staged, and the complex
 // product is formed from real bf16 MMAs with FP32 accumulation.
 //
-// Complex -> real mapping (one MMA per pair of planes and k-step):
+// Complex -> real mapping for a tile of RT right-hand sides:
 //   A_real (128 rows x 2n) : row m = Re a_m0, Im a_m0, Re a_m1, Im a_m1, ...
-//   B      (2n x 32)       : rows 2j, 2j+1 of column q   = ( Re x_jq, -Im x_jq)
-//                            rows 2j, 2j+1 of column 16+q = ( Im x_jq,  Re x_jq)
-//   D = A_real B           : column q = Re y_q, column 16+q = Im y_q
+//   B      (2n x 2 RT)     : rows 2j, 2j+1 of column q    = ( Re x_jq, -Im x_jq)
+//                            rows 2j, 2j+1 of column RT+q = ( Im x_jq,  Re x_jq)
+//   D = A_real B           : column q = Re y_q, column RT+q = Im y_q
 // so the stored block needs no duplication and the output lands in TMEM as
 // one row per lane.
 //
 // Products kept: TERMS = 2 -> hh + hl + lh (bf16x2, ~16 significant bits);
 // TERMS = 3 -> additionally h l2 + l l + l2 h (bf16x3, ~24 bits, FP32-like).
+// Two tile widths: RT = 16 (up to 16 RHS) and RT = 32 (more RHS: half the
+// chunk passes per right-hand side, with MMAs of N = 128).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -30,37 +32,59 @@ namespace {
 // barriers are waited on by one MMA thread, in order (an mbarrier parity wait
 // must not run more than one phase ahead of the barrier)
 constexpr int kTcStages = 4;
-constexpr int kTcRhs = 16;                 // RHS per CTA
-constexpr int kTcN = 2 * kTcRhs;           // MMA N: real and imaginary columns
 constexpr int kAPlaneBytes = 64 * 128;     // at most 64 core matrices per plane
-constexpr int kBPlaneBytes = (kTcChunkCols / 4) * (kTcN / 8) * 128;      // 8 KB
-constexpr int kBuilders = 128;             // warps 0-3: B planes
-constexpr int kExtractors = 128;           // warps 4-7: TMEM partial sums and stores
-constexpr int kProducerWarp = (kBuilders + kExtractors) / 32, kMmaWarp = kProducerWarp + 1;
-// + one bulk-copy warp + two MMA warps (even / odd chunks)
-constexpr int kTcThreads = kBuilders + kExtractors + 96;
 constexpr uint64_t kWaitLimitNs = 1000000000ull;                          // 1 s
 
-constexpr int kXStageBytes = kTcChunkCols * kTcRhs * 8;                   // 8 KB
 constexpr int32_t kTcBulkX = 1, kTcBulkW = 2;   // inputs / intermediates by bulk copy
 
-template <int TERMS>
+template <int TERMS, int RT>
 struct TcLayout {
-  // B planes interleaved by k-group: k-group g holds plane 0's four n-groups,
-  // then plane 1's, ... so that planes u .. TERMS-1 form one N = 32 (TERMS-u)
-  // operand; bytes of one k-group:
-  static constexpr int kBKGroupBytes = TERMS * (kTcN / 8) * 128;
+  static_assert(RT == 16 || RT == 32, "RHS tile");
+  static constexpr int kN = 2 * RT;        // D columns of one product group
+  // B planes interleaved by k-group: k-group g holds plane 0's kN / 8
+  // n-groups, then plane 1's, ... so that planes u .. TERMS-1 form one
+  // N = kN (TERMS-u) operand; bytes of one plane and of one k-group:
+  static constexpr int kBPlaneKGroupBytes = (kN / 8) * 128;
+  static constexpr int kBKGroupBytes = TERMS * kBPlaneKGroupBytes;
+  // product groups in TMEM per accumulator chain: unfolded (RT = 16), one
+  // group per B plane (one MMA per A plane and k-step, N = 32 TERMS ... 32);
+  // folded (RT = 32), the products with B planes 1 and 2 share one group
+  // (N <= 128)
+  static constexpr bool kFold = RT == 32;
+  static constexpr int kGroups = kFold ? 2 : TERMS;
+  static_assert(kGroups * kN <= 128, "TMEM columns of one chain");
+  // TMEM: kNB accumulator buffers (chunk i uses buffer i % kNB) of kNC
+  // k-step chains (k-step st adds to chain st % kNC), 128 columns each;
+  // buffer b chain c at column 128 (b + kNB c).  RT = 32: four buffers of
+  // one chain (two buffers of two chains: 7 % slower at 256 RHS, error
+  // 4.1e-7 instead of 6.2e-7 at 65,536 points)
+  static constexpr int kNB = RT == 32 ? 4 : 2, kNC = RT == 32 ? 1 : 2;
+  static_assert(kNB * kNC * 128 <= 512, "TMEM columns");
+  static constexpr int kXStageBytes = kTcChunkCols * RT * 8;
+  // warp roles: builders (B planes), extractors (TMEM partial sums and
+  // stores; 16 RHS of one TMEM lane quarter each), one bulk-copy warp and
+  // the two MMA warps (the even and the odd chunks: one thread's waits and
+  // descriptor work overlap the other's MMAs).  RT = 16: 4 + 4 + 1 + 2
+  // warps; RT = 32: 4 + 8 + 1 + 2 warps (the extractors' accumulators of 32
+  // RHS would not fit one thread's registers; measured at 256 RHS, two
+  // builder warps were 12 % and one MMA warp 7 % slower)
+  static constexpr int kBuilders = 128;
+  static constexpr int kExtractors = RT == 16 ? 128 : 256;
+  static constexpr int kMmaWarps = 2;
+  static constexpr int kProducerWarp = (kBuilders + kExtractors) / 32;
+  static constexpr int kMmaWarp = kProducerWarp + 1;
+  static constexpr int kThreads = kBuilders + kExtractors + 32 * (1 + kMmaWarps);
   static constexpr int aBytes = TERMS * kAPlaneBytes;
-  static constexpr int bBytes = TERMS * kBPlaneBytes;
+  static constexpr int bBytes = (kTcChunkCols / 4) * kBKGroupBytes;
   // A planes, B planes, then the chunk's FP32 right-hand sides
   static constexpr int stageBytes = aBytes + bBytes + kXStageBytes;
   // an A descriptor spans 16 row groups and the last k-step reads up to 2 KB
   // past a short tile (rows whose outputs are discarded): 2 KB of slack
   // follow the last stage
   static constexpr int barOff = kTcStages * stageBytes + 2048;
-  // fullA[S], fullB[S], empty[S], accFull[2], accEmpty[2], fullX[S], TMEM
-  // slot, abort
-  static constexpr int smemBytes = barOff + 8 * (4 * kTcStages + 4) + 16;
+  // fullA[S], fullB[S], empty[S], accFull[kNB], accEmpty[kNB], fullX[S],
+  // TMEM slot, abort
+  static constexpr int smemBytes = barOff + 8 * (4 * kTcStages + 2 * kNB) + 16;
   static_assert(smemBytes <= 232448, "shared memory per CTA");
   static_assert(kTcStages % 2 == 0, "stages must hold one chunk parity each");
 };
@@ -108,6 +132,19 @@ __device__ __forceinline__ bool mbarTryWait(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+// the same test, letting the hardware suspend the thread for up to 2 us
+// while the phase is incomplete (it resumes as soon as the phase completes)
+__device__ __forceinline__ bool mbarTryWaitSuspend(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity), "n"(2000)
+      : "memory");
+  return ok != 0;
+}
 __device__ __forceinline__ uint64_t globalTimerNs() {
   uint64_t t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -123,7 +160,11 @@ __device__ bool mbarWait(uint32_t bar, uint32_t parity, int volatile *abort, uin
   if (mbarTryWait(bar, parity)) return true;
   uint64_t const t0 = globalTimerNs();
   for (;;) {
-    if (mbarTryWait(bar, parity)) return true;
+    // the abort flag and the clock are read every 8 suspended tests, not
+    // every test: polling warps take fewer issue slots from working ones
+#pragma unroll 1
+    for (int k = 0; k < 8; ++k)
+      if (mbarTryWaitSuspend(bar, parity)) return true;
     if (*abort || globalTimerNs() - t0 > limitNs) return false;
   }
 }
@@ -155,8 +196,8 @@ __device__ __forceinline__ void fenceProxyAsync() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-// the whole tensor memory (one CTA per SM): two accumulator buffers x two
-// k-step chains of up to 96 FP32 columns, buffer b chain c at column 128 b + 256 c
+// the whole tensor memory (one CTA per SM): the accumulator buffers and
+// k-step chains of TcLayout, 128 columns each
 __device__ __forceinline__ void tmemAlloc512(uint32_t slot) {
   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(slot)
                : "memory");
@@ -222,6 +263,30 @@ __device__ __forceinline__ void tmemLoad8(uint32_t taddr, float *v) {
 #pragma unroll
   for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
+// 16 consecutive FP32 columns of this thread's TMEM lane (no wait)
+__device__ __forceinline__ void tmemLoad16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+// (a.x + b.x, a.y + b.y), both rounded to nearest: one packed FP32 add
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+  uint64_t ra, rb, r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(ra) : "f"(a.x), "f"(a.y));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(rb) : "f"(b.x), "f"(b.y));
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(ra), "l"(rb));
+  float2 o;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(o.x), "=f"(o.y) : "l"(r));
+  return o;
+}
 __device__ __forceinline__ void tmemWaitLoads() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
@@ -255,8 +320,9 @@ __global__ void __launch_bounds__(256) tcFillKernel(TcFill const *__restrict__ f
   }
 }
 
-// Persistent CTA over its chunk stream (one apply stage, one tile of 16 RHS),
-// warp-specialised around mbarriers:
+// Persistent CTA over its chunk stream (one apply stage, one tile of RT RHS),
+// warp-specialised around mbarriers (warp numbers for RT = 16; TcLayout
+// gives both layouts):
 //   warp 8           once the MMAs of chunk i-4 are done (empty) bulk-copies
 //                    chunk i's FP32 right-hand-side rows when they form one
 //                    aligned block (fullX), then its A planes into stage
@@ -264,25 +330,29 @@ __global__ void __launch_bounds__(256) tcFillKernel(TcFill const *__restrict__ f
 //   warps 0-3        otherwise copy chunk i+2's right-hand sides into its
 //                    stage (cp.async); build chunk i's bf16 B planes (fullB);
 //   warps 9, 10      (lane 0) issue the MMAs of the even and the odd chunks,
-//                    chunk i into TMEM buffer i % 2, once its A and B planes
-//                    have landed and the buffer was read;
+//                    chunk i into TMEM buffer i % kNB, once its A and B
+//                    planes have landed and the buffer was read;
 //   warps 4-7        read each chunk's partial sums from TMEM (accFull) into
 //                    FP32 registers, release the buffer (accEmpty) and store
 //                    finished items.
-// Each chunk starts its TMEM buffer from zero and alternates its k-steps
-// between two accumulator chains, so the tensor cores accumulate at most 4
-// k-steps before the sums move to FP32 registers (the tensor-core FP32
+// Each chunk starts its TMEM buffer from zero and deals its k-steps to the
+// buffer's kNC accumulator chains, so the tensor cores accumulate only a
+// few k-steps before the sums move to FP32 registers (the tensor-core FP32
 // accumulation loses accuracy over long chains).
 // Every wait is bounded (kWaitLimitNs) and gives up when another role has;
 // the CTA then waits (bounded) for the copies and MMAs it has in flight,
 // frees its TMEM and reports kStatusTcTimeout.
-template <int TERMS>
-__global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
+template <int TERMS, int RT>
+__global__ void __launch_bounds__(TcLayout<TERMS, RT>::kThreads, 1) applyTcKernel(
     TcChunk const *__restrict__ chunks, int64_t const *__restrict__ ctaChunk0,
     uint8_t const *__restrict__ tarena, float2 const *__restrict__ X, int64_t ldx,
     float2 *__restrict__ W, int64_t R, int32_t rhsTiles, int32_t xBulk, uint64_t waitLimitNs,
     int32_t *status) {
-  using L = TcLayout<TERMS>;
+  using L = TcLayout<TERMS, RT>;
+  constexpr int kN = L::kN;
+  constexpr int kBuilders = L::kBuilders, kExtractors = L::kExtractors;
+  constexpr int kProducerWarp = L::kProducerWarp, kMmaWarp = L::kMmaWarp;
+  constexpr int kMmaWarps = L::kMmaWarps;
   constexpr int S = kTcStages;
   constexpr int kBKGroupBytes = L::kBKGroupBytes;
   extern __shared__ __align__(1024) uint8_t smem[];
@@ -295,21 +365,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
   int64_t const c0 = ctaChunk0[stream];
   int64_t const nCh = ctaChunk0[stream + 1] - c0;
   if (nCh <= 0) return;
-  int64_t const r0 = (int64_t)tile * kTcRhs;
-  int const nr = (R - r0) < kTcRhs ? (int)(R - r0) : kTcRhs;
+  int64_t const r0 = (int64_t)tile * RT;
+  int const nr = (R - r0) < RT ? (int)(R - r0) : RT;
   TcChunk const *ch = chunks + c0;
   // a chunk's right-hand sides arrive by one bulk copy with its A planes when
-  // they form a contiguous 16-byte aligned block (16 RHS, leading dimension
-  // 16), else by the builders' cp.async (one copy per 128 B row was slower:
+  // they form a contiguous 16-byte aligned block (RT RHS, leading dimension
+  // RT), else by the builders' cp.async (one copy per 128 B row was slower:
   // the copy engine takes small copies one at a time)
-  bool const bulkX = nr == kTcRhs && (xBulk & kTcBulkX);
-  bool const bulkW = nr == kTcRhs && (xBulk & kTcBulkW);
+  bool const bulkX = nr == RT && (xBulk & kTcBulkX);
+  bool const bulkW = nr == RT && (xBulk & kTcBulkW);
 
   uint32_t const sbase = smemAddr(smem);
   uint32_t const fullA = sbase + L::barOff, fullB = fullA + 8 * S, empty = fullB + 8 * S;
-  uint32_t const accFull = empty + 8 * S, accEmpty = accFull + 16;
-  uint32_t const fullX = accEmpty + 16;
-  uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(smem + L::barOff + 8 * (4 * S + 4));
+  constexpr int NB = L::kNB, NC = L::kNC;
+  uint32_t const accFull = empty + 8 * S, accEmpty = accFull + 8 * NB;
+  uint32_t const fullX = accEmpty + 8 * NB;
+  uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(smem + L::barOff + 8 * (4 * S + 2 * NB));
   int volatile *abortFlag = reinterpret_cast<int volatile *>(tmemSlot + 1);
 
   if (tid == 0) {
@@ -319,7 +390,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
       mbarInit(fullB + 8 * s, kBuilders / 32);
       mbarInit(empty + 8 * s, 1);
     }
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < NB; ++b) {
       mbarInit(accFull + 8 * b, 1);
       mbarInit(accEmpty + 8 * b, kExtractors / 32);
     }
@@ -365,11 +436,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
         // the input rows first, on their own barrier (every chunk arrives on
         // it, with no bytes on the cp.async path, so its phases follow the
         // chunks): the builders convert them while the A planes stream in
-        mbarExpectTx(fullX + 8 * s, bulk ? (uint32_t)nc * 128 : 0u);
-        // the chunk's input rows are one contiguous block (leading dimension 16)
+        mbarExpectTx(fullX + 8 * s, bulk ? (uint32_t)nc * (RT * 8) : 0u);
+        // the chunk's input rows are one contiguous block (leading dimension RT)
         if (bulk)
           bulkG2S(sbase + s * L::stageBytes + L::aBytes + L::bBytes,
-                  (inIsX ? X : W) + inRow * kTcRhs, (uint32_t)nc * (kTcRhs * 8), fullX + 8 * s);
+                  (inIsX ? X : W) + inRow * RT, (uint32_t)nc * (RT * 8), fullX + 8 * s);
         mbarExpectTx(fullA + 8 * s, plane * TERMS);
 #pragma unroll
         for (int t = 0; t < TERMS; ++t)
@@ -384,24 +455,25 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
       nc = ncN;
       inIsX = inIsXN;
     }
-  } else if (warp == kMmaWarp || warp == kMmaWarp + 1) {
-    // ---- MMAs: warp kMmaWarp issues the even chunks, the next warp the odd
-    // ones, so one thread's waits and bookkeeping overlap the other's MMAs in
-    // the tensor pipe; chunk i uses TMEM buffer i % 2, i.e. its thread's own ----
+  } else if (warp >= kMmaWarp) {
+    // ---- MMAs: with two MMA warps, warp kMmaWarp issues the even chunks and
+    // the next warp the odd ones, so one thread's waits and bookkeeping
+    // overlap the other's MMAs in the tensor pipe; chunk i uses TMEM buffer
+    // i % kNB ----
     int const parity = warp - kMmaWarp;
     if (lane == 0 && parity < nCh) {
 
       int32_t kg = ch[parity].kg, mg = ch[parity].mg;
-      for (int64_t i = parity; i < nCh; i += 2) {
-        int const s = (int)(i % S), b = (int)(i & 1);
+      for (int64_t i = parity; i < nCh; i += kMmaWarps) {
+        int const s = (int)(i % S), b = (int)(i % NB);
         uint32_t const ph = (uint32_t)((i / S) & 1);
         int32_t kgN = 0, mgN = 0;
-        if (i + 2 < nCh) {
-          kgN = ch[i + 2].kg;
-          mgN = ch[i + 2].mg;
+        if (i + kMmaWarps < nCh) {
+          kgN = ch[i + kMmaWarps].kg;
+          mgN = ch[i + kMmaWarps].mg;
         }
         if (!mbarWait(fullA + 8 * s, ph, abortFlag, waitLimitNs) || !mbarWait(fullB + 8 * s, ph, abortFlag, waitLimitNs) ||
-            (i >= 2 && !mbarWait(accEmpty + 8 * b, (uint32_t)(((i >> 1) - 1) & 1), abortFlag, waitLimitNs))) {
+            (i >= NB && !mbarWait(accEmpty + 8 * b, (uint32_t)((i / NB - 1) & 1), abortFlag, waitLimitNs))) {
           *abortFlag = 1;
           break;
         }
@@ -410,25 +482,42 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
         uint32_t const lboA = (uint32_t)mg * 128;
         int const ksteps = (kg + 1) >> 1;
         int const mRows = mg <= 8 ? 64 : 128;
-        // A plane t times the B planes 0 .. TERMS-1-t, side by side in N: D
-        // columns 32 u .. 32 u + 31 collect the products with B plane u.  The
-        // descriptors of k-step st are those of k-step 0 with the start
+        // The descriptors of k-step st are those of k-step 0 with the start
         // address advanced (the address field is the low 14 bits, in 16 B).
         uint64_t da[TERMS];
 #pragma unroll
         for (int t = 0; t < TERMS; ++t) da[t] = smemDesc(aS + t * kAPlaneBytes, lboA, 128);
         uint64_t db = smemDesc(bS, kBKGroupBytes, 128);
         uint64_t const stepA = (2 * lboA) >> 4, stepB = (2 * kBKGroupBytes) >> 4;
+        // B plane u of the k-group, as a descriptor offset
+        constexpr uint64_t kBPlane = (uint64_t)L::kBPlaneKGroupBytes >> 4;
         uint32_t const d = tmem + 128 * b;
 #pragma unroll
         for (int st = 0; st < kTcChunkCols / 8; ++st) {
           if (st >= ksteps) break;
-          uint32_t const dc = d + 256 * (st & 1);   // even / odd k-step chain
+          uint32_t const dc = d + 128 * NB * (st % NC);   // the k-step's chain
+          uint32_t const acc0 = st >= NC ? 1u : 0u;       // a chain's first k-step overwrites
+          if constexpr (!L::kFold) {
+            // A plane t times the B planes 0 .. TERMS-1-t, side by side in
+            // N: D columns 32 u .. 32 u + 31 collect the products with B
+            // plane u
 #pragma unroll
-          for (int t = 0; t < TERMS; ++t) {
-            tcMma(dc, da[t], db, idesc(mRows, kTcN * (TERMS - t)), (st >= 2 || t > 0) ? 1u : 0u);
-            da[t] += stepA;
+            for (int t = 0; t < TERMS; ++t)
+              tcMma(dc, da[t], db, idesc(mRows, kN * (TERMS - t)), (acc0 || t > 0) ? 1u : 0u);
+          } else if constexpr (TERMS == 3) {
+            // group 0 (columns 0 .. kN-1) collects the products with B plane
+            // 0, group 1 those with B planes 1 and 2 (hm + mm + hl); the
+            // smallest products go first, hh last
+            tcMma(dc, da[1], db, idesc(mRows, 2 * kN), acc0);             // m x (h | m)
+            tcMma(dc, da[2], db, idesc(mRows, kN), 1u);                   // l x h
+            tcMma(dc + kN, da[0], db + 2 * kBPlane, idesc(mRows, kN), 1u);  // h x l
+            tcMma(dc, da[0], db, idesc(mRows, 2 * kN), 1u);               // h x (h | m)
+          } else {
+            tcMma(dc, da[0], db, idesc(mRows, 2 * kN), acc0);             // h x (h | l)
+            tcMma(dc, da[1], db, idesc(mRows, kN), 1u);                   // l x h
           }
+#pragma unroll
+          for (int t = 0; t < TERMS; ++t) da[t] += stepA;
           db += stepB;
         }
         tcCommit(empty + 8 * s);
@@ -466,24 +555,27 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
     if (tid < kBuilders) {
       // ---- B planes ----
       // A builder converts columns j0 .. j0+3 (j0 = 4 jg: one k-group) of RHS
-      // q, jg = (lane >> 4) + 2 warp + 8 p for passes p = 0, 1: the four
+      // q = tid % RT, jg = tid / RT + kJgPass p for passes p: the four
       // complex values fill one 16 B core-matrix row of each B plane, and a
       // warp's stores cover 512 contiguous-in-banks bytes.  On the cp.async
       // path the thread that copies an element into the X stage is the one
       // that converts it, so the cp.async groups need no barrier.
       // Descriptors are loaded one iteration before their first use.
-      int const q = lane & 15, jgBase = (lane >> 4) + 2 * warp;
+      constexpr int kJgPass = kBuilders / RT;               // k-groups per pass
+      constexpr int kPasses = (kTcChunkCols / 4) / kJgPass;
+      static_assert(kPasses * kJgPass == kTcChunkCols / 4, "builder passes");
+      int const q = tid % RT, jgBase = tid / RT;
       auto issueX = [&](Cd const &d, int64_t i) {
         int64_t const xld = d.inIsX ? ldx : R;
         float2 const *src = (d.inIsX ? X : W) + d.inRow * xld + r0 + q;
         uint32_t const xs = sbase + (int)(i % S) * L::stageBytes + L::aBytes + L::bBytes;
         if (q < nr)
 #pragma unroll
-          for (int p = 0; p < 2; ++p)
+          for (int p = 0; p < kPasses; ++p)
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-              int const j = 4 * (jgBase + 8 * p) + u;
-              if (j < d.nc) cpAsync8(xs + (uint32_t)(j * kTcRhs + q) * 8, src + (int64_t)j * xld);
+              int const j = 4 * (jgBase + kJgPass * p) + u;
+              if (j < d.nc) cpAsync8(xs + (uint32_t)(j * RT + q) * 8, src + (int64_t)j * xld);
             }
       };
       auto bulkOf = [&](Cd const &d) { return d.inIsX ? bulkX : bulkW; };
@@ -523,14 +615,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
         float2 const *xs = reinterpret_cast<float2 const *>(stage + L::aBytes + L::bBytes);
         int const kgEven = ((d0.kg + 1) >> 1) * 2;   // k-groups the MMAs read
 #pragma unroll
-        for (int p = 0; p < 2; ++p) {
-          int const jg = jgBase + 8 * p;
+        for (int p = 0; p < kPasses; ++p) {
+          int const jg = jgBase + kJgPass * p;
           if (jg < kgEven) {
             float2 v[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
               int const j = 4 * jg + u;
-              v[u] = (j < d0.nc && q < nr) ? xs[j * kTcRhs + q] : make_float2(0.f, 0.f);
+              v[u] = (j < d0.nc && q < nr) ? xs[j * RT + q] : make_float2(0.f, 0.f);
             }
             uint32_t pr[4][TERMS];
 #pragma unroll
@@ -538,12 +630,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
             uint32_t const offRe = (uint32_t)jg * kBKGroupBytes + (q >> 3) * 128 + (q & 7) * 16;
 #pragma unroll
             for (int t = 0; t < TERMS; ++t) {
-              // rows 2j, 2j+1 of column q: (Re x, -Im x); of column 16+q
-              // (two core rows further): (Im x, Re x)
-              *reinterpret_cast<uint4 *>(bsm + t * 512 + offRe) =
+              // rows 2j, 2j+1 of column q: (Re x, -Im x); of column RT+q
+              // (RT / 8 core rows further): (Im x, Re x)
+              uint8_t *bp = bsm + t * L::kBPlaneKGroupBytes + offRe;
+              *reinterpret_cast<uint4 *>(bp) =
                   make_uint4(pr[0][t] ^ 0x80000000u, pr[1][t] ^ 0x80000000u,
                              pr[2][t] ^ 0x80000000u, pr[3][t] ^ 0x80000000u);
-              *reinterpret_cast<uint4 *>(bsm + t * 512 + offRe + 2 * 128) =
+              *reinterpret_cast<uint4 *>(bp + (RT / 8) * 128) =
                   make_uint4(__byte_perm(pr[0][t], 0, 0x1032), __byte_perm(pr[1][t], 0, 0x1032),
                              __byte_perm(pr[2][t], 0, 0x1032), __byte_perm(pr[3][t], 0, 0x1032));
             }
@@ -569,37 +662,58 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
       cpAsyncWait<0>();
     } else {
       // ---- TMEM partial sums, FP32 accumulation, stores ----
-      // extractor warp e reads TMEM lane quarter e: item row 32 e + lane
+      // extractor warp w reads TMEM lane quarter w % 4 (item row
+      // 32 (w % 4) + lane) for the 16 RHS 16 h .. 16 h + 15 of the tile,
+      // h = (w - first extractor warp) / 4
       int const e = warp & 3;
-      float acc[2 * kTcRhs];   // RHS 0..15 real parts, then imaginary parts
+      int const h = (warp - kBuilders / 32) >> 2;
+      float acc[32];   // 16 real parts, then 16 imaginary parts
 #pragma unroll
-      for (int c = 0; c < 2 * kTcRhs; ++c) acc[c] = 0.f;
+      for (int c = 0; c < 32; ++c) acc[c] = 0.f;
+      // TMEM columns per load: 8 for three groups, 16 for two; one wait per
+      // part.  Part p covers accumulator slots
+      // kLoadW p ..: real parts (columns 16 h + ..) then imaginary parts
+      // (columns RT + 16 h + ..)
+      constexpr int kLoadW = L::kGroups == 3 ? 8 : 16, kG = L::kGroups;
       Ce dn = loadCe(0);
       for (int64_t j = 0; j < nCh; ++j) {
         Ce const d = dn;
         dn = loadCe(j + 1);
-        int const b = (int)(j & 1);
+        int const b = (int)(j % NB);
         // as one warp (a vote), for the collective TMEM loads below
-        if (!__all_sync(0xffffffffu, mbarWait(accFull + 8 * b, (uint32_t)((j >> 1) & 1), abortFlag, waitLimitNs))) {
+        if (!__all_sync(0xffffffffu, mbarWait(accFull + 8 * b, (uint32_t)((j / NB) & 1), abortFlag, waitLimitNs))) {
           *abortFlag = 1;
           break;
         }
         tcFenceAfter();
         uint32_t const tl = tmem + 128 * b + ((uint32_t)(e * 32) << 16);
-        int const chains = d.kg > 2 ? 2 : 1;   // the odd k-step chain was written
+        int const ksteps = (d.kg + 1) >> 1;
+        int const chains = ksteps < NC ? ksteps : NC;   // the chains this chunk wrote
         for (int c = 0; c < chains; ++c) {
 #pragma unroll
-          for (int part = 0; part < 4; ++part) {   // columns 8 part .. 8 part + 7 of each group
-            float v[TERMS][8];
+          for (int part = 0; part < 32 / kLoadW; ++part) {
+            int const slot = kLoadW * part;
+            uint32_t const col = slot < 16 ? 16 * h + slot : RT + 16 * h + (slot - 16);
+            float v[kG][kLoadW];
 #pragma unroll
-            for (int u = 0; u < TERMS; ++u) tmemLoad8(tl + 256 * c + 32 * u + 8 * part, v[u]);
+            for (int u = 0; u < kG; ++u) {
+              uint32_t const ta = tl + 128 * NB * c + kN * u + col;
+              if constexpr (kLoadW == 8)
+                tmemLoad8(ta, v[u]);
+              else
+                tmemLoad16(ta, v[u]);
+            }
             tmemWaitLoads();
+            // the group of the smaller products first; packed adds, the same
+            // roundings as scalar ones
 #pragma unroll
-            for (int k = 0; k < 8; ++k) {
-              float t = v[TERMS - 1][k];   // products with the smallest B plane first
+            for (int k = 0; k < kLoadW; k += 2) {
+              float2 t = make_float2(v[kG - 1][k], v[kG - 1][k + 1]);
 #pragma unroll
-              for (int u = TERMS - 2; u >= 0; --u) t += v[u][k];
-              acc[8 * part + k] += t;
+              for (int u = kG - 2; u >= 0; --u) t = add2(t, make_float2(v[u][k], v[u][k + 1]));
+              float2 const a = add2(make_float2(acc[slot + k], acc[slot + k + 1]), t);
+              acc[slot + k] = a.x;
+              acc[slot + k + 1] = a.y;
             }
           }
         }
@@ -610,13 +724,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
           // M = 64 chunks (items of <= 64 rows): lanes 16..31 hold no row
           int const row = d.rows <= 64 ? (lane < 16 ? e * 16 + lane : kTcRows) : e * 32 + lane;
           if (row < d.rows) {
-            float2 *out = W + (d.outRow + row) * R + r0;
+            float2 *out = W + (d.outRow + row) * R + r0 + 16 * h;
 #pragma unroll
-            for (int c = 0; c < kTcRhs; ++c)
-              if (c < nr) out[c] = make_float2(acc[c], acc[kTcRhs + c]);
+            for (int c = 0; c < 16; ++c)
+              if (16 * h + c < nr) out[c] = make_float2(acc[c], acc[16 + c]);
           }
 #pragma unroll
-          for (int c = 0; c < 2 * kTcRhs; ++c) acc[c] = 0.f;
+          for (int c = 0; c < 32; ++c) acc[c] = 0.f;
         }
       }
     }
@@ -635,7 +749,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
         mbarDrain(fullX + 8 * (j % S), (uint32_t)((j / S) & 1));
         mbarDrain(fullA + 8 * (j % S), (uint32_t)((j / S) & 1));
       }
-    if ((warp == kMmaWarp || warp == kMmaWarp + 1) && lane == 0 && lastMma >= 0)
+    if (warp >= kMmaWarp && lane == 0 && lastMma >= 0)
       mbarDrain(empty + 8 * (lastMma % S), (uint32_t)((lastMma / S) & 1));
   }
   tcFenceBefore();
@@ -650,28 +764,38 @@ __global__ void __launch_bounds__(kTcThreads, 1) applyTcKernel(
 
 }  // namespace
 
-int32_t tcSmemBytes(int32_t terms) {
-  return terms == 3 ? TcLayout<3>::smemBytes : TcLayout<2>::smemBytes;
-}
+// the RHS tile of an apply of R right-hand sides
+int32_t tcRhsTile(int64_t R) { return R > 16 ? 32 : 16; }
 
-cudaError_t tcPrepare(int32_t terms, int32_t *ctasPerSm) {
-  cudaError_t e;
-  int per = 0;
-  if (terms == 3) {
-    e = cudaFuncSetAttribute(applyTcKernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             TcLayout<3>::smemBytes);
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, applyTcKernel<3>, kTcThreads,
-                                                      TcLayout<3>::smemBytes);
-  } else {
-    e = cudaFuncSetAttribute(applyTcKernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             TcLayout<2>::smemBytes);
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, applyTcKernel<2>, kTcThreads,
-                                                      TcLayout<2>::smemBytes);
-  }
+namespace {
+template <int TERMS, int RT>
+cudaError_t prepareOne(int *per) {
+  cudaError_t e = cudaFuncSetAttribute(applyTcKernel<TERMS, RT>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       TcLayout<TERMS, RT>::smemBytes);
   if (e != cudaSuccess) return e;
-  *ctasPerSm = per;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, applyTcKernel<TERMS, RT>,
+                                                       TcLayout<TERMS, RT>::kThreads,
+                                                       TcLayout<TERMS, RT>::smemBytes);
+}
+template <int TERMS, int RT>
+void launchOne(dim3 grid, cudaStream_t stream, TcChunk const *chunks, int64_t const *ctaChunk0,
+               uint8_t const *tarena, float2 const *X, int64_t ldx, float2 *W, int64_t R,
+               int32_t tiles, int32_t xBulk, uint64_t waitLimitNs, int32_t *status) {
+  applyTcKernel<TERMS, RT><<<grid, TcLayout<TERMS, RT>::kThreads, TcLayout<TERMS, RT>::smemBytes,
+                             stream>>>(
+      chunks, ctaChunk0, tarena, X, ldx, W, R, tiles, xBulk, waitLimitNs, status);
+}
+}  // namespace
+
+// resident CTAs per SM of every tile width (the smaller count)
+cudaError_t tcPrepare(int32_t terms, int32_t *ctasPerSm) {
+  int a = 0, b = 0;
+  cudaError_t e = terms == 3 ? prepareOne<3, 16>(&a) : prepareOne<2, 16>(&a);
+  if (e != cudaSuccess) return e;
+  e = terms == 3 ? prepareOne<3, 32>(&b) : prepareOne<2, 32>(&b);
+  if (e != cudaSuccess) return e;
+  *ctasPerSm = a < b ? a : b;
   return cudaSuccess;
 }
 
@@ -691,18 +815,26 @@ cudaError_t launchApplyTc(int32_t terms, TcChunk const *chunks, int64_t const *c
                           float2 *W, int64_t R, int32_t *status, cudaStream_t stream,
                           uint64_t waitLimitNs) {
   if (ctas == 0) return cudaSuccess;
-  int64_t const tiles = (R + kTcRhs - 1) / kTcRhs;
+  int32_t const rt = tcRhsTile(R);
+  int64_t const tiles = (R + rt - 1) / rt;
   if (tiles > 0x7fffffff / ctas) return cudaErrorInvalidValue;
   dim3 grid((unsigned)(ctas * tiles));
-  // one bulk copy per chunk: 16 RHS with leading dimension 16, 16-byte aligned
-  int32_t const xBulk = ((R == kTcRhs && ldx == kTcRhs && (uintptr_t)X % 16 == 0) ? kTcBulkX : 0) |
-                        ((R == kTcRhs && (uintptr_t)W % 16 == 0) ? kTcBulkW : 0);
-  if (terms == 3)
-    applyTcKernel<3><<<grid, kTcThreads, TcLayout<3>::smemBytes, stream>>>(
-        chunks, ctaChunk0, tarena, X, ldx, W, R, (int32_t)tiles, xBulk, waitLimitNs, status);
+  // one bulk copy per chunk: RT RHS with leading dimension RT, 16-byte aligned
+  int32_t const xBulk = ((R == rt && ldx == rt && (uintptr_t)X % 16 == 0) ? kTcBulkX : 0) |
+                        ((R == rt && (uintptr_t)W % 16 == 0) ? kTcBulkW : 0);
+  auto const t32 = (int32_t)tiles;
+  if (terms == 3 && rt == 16)
+    launchOne<3, 16>(grid, stream, chunks, ctaChunk0, tarena, X, ldx, W, R, t32, xBulk,
+                     waitLimitNs, status);
+  else if (terms == 3)
+    launchOne<3, 32>(grid, stream, chunks, ctaChunk0, tarena, X, ldx, W, R, t32, xBulk,
+                     waitLimitNs, status);
+  else if (rt == 16)
+    launchOne<2, 16>(grid, stream, chunks, ctaChunk0, tarena, X, ldx, W, R, t32, xBulk,
+                     waitLimitNs, status);
   else
-    applyTcKernel<2><<<grid, kTcThreads, TcLayout<2>::smemBytes, stream>>>(
-        chunks, ctaChunk0, tarena, X, ldx, W, R, (int32_t)tiles, xBulk, waitLimitNs, status);
+    launchOne<2, 32>(grid, stream, chunks, ctaChunk0, tarena, X, ldx, W, R, t32, xBulk,
+                     waitLimitNs, status);
   return cudaGetLastError();
 }
 

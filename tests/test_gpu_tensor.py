@@ -42,7 +42,7 @@ def golden_fac(name, ctx):
 
 
 @pytest.mark.parametrize("prec", ["bf16x3", "bf16x2"])
-@pytest.mark.parametrize("R", [1, 5, 16, 40])
+@pytest.mark.parametrize("R", [1, 5, 16, 40, 64])
 def test_tensor_apply_close_to_fp64(ctx, prec, R):
     g, fac = golden_fac("c1_circle_n4096_k64", ctx)
     X = O.RefRng(11 + R).complex_randn(4096 * R).reshape(4096, R)
@@ -70,16 +70,30 @@ def test_tensor_apply_is_deterministic(ctx):
     assert torch.equal(y1, y2)
 
 
-def test_tensor_apply_columns_are_independent(ctx):
-    """RHS tiles of 16 and the partial last tile give each column the result
-    of its own single-column apply."""
+@pytest.mark.parametrize("prec", ["bf16x3", "bf16x2"])
+def test_tensor_apply_columns_are_independent(ctx, prec):
+    """Within one tile width (16 RHS for R <= 16, 32 above) a column's
+    result depends on nothing but that column: not on its place in the tile,
+    its neighbours or the partial last tile.  The two widths sum the plane
+    products in different groupings, so across them the results agree to
+    rounding."""
     g, fac = golden_fac("star_n2048_k48", ctx)
-    X = O.RefRng(4).complex_randn(2048 * 21).reshape(2048, 21)
+    X = O.RefRng(4).complex_randn(2048 * 45).reshape(2048, 45)
     Xd = torch.from_numpy(X).cuda().to(torch.complex64)
-    y = fac.apply(Xd, precision="bf16x3").cpu().numpy()
-    for c in (0, 15, 16, 20):
-        yc = fac.apply(Xd[:, c:c + 1].contiguous(), precision="bf16x3").cpu().numpy()
-        assert np.array_equal(y[:, c:c + 1], yc)
+    # 16-RHS tiles: R = 13 against single columns
+    y13 = fac.apply(Xd[:, :13].contiguous(), precision=prec).cpu().numpy()
+    for c in (0, 7, 12):
+        yc = fac.apply(Xd[:, c:c + 1].contiguous(), precision=prec).cpu().numpy()
+        assert np.array_equal(y13[:, c:c + 1], yc)
+    # 32-RHS tiles: R = 45 (a partial second tile) against R = 17 applies
+    # holding the column first
+    y45 = fac.apply(Xd, precision=prec).cpu().numpy()
+    for c in (0, 15, 16, 31, 32, 44):
+        Xc = torch.cat([Xd[:, c:c + 1], Xd[:, 20:36]], dim=1).contiguous()
+        yc = fac.apply(Xc, precision=prec).cpu().numpy()
+        assert np.array_equal(y45[:, c:c + 1], yc[:, :1])
+    assert rel_err(y45[:, :13].astype(np.complex128), y13.astype(np.complex128)) < \
+        TOL[prec] / 3
 
 
 def test_tensor_apply_host_operands_and_original_order(ctx):
@@ -157,14 +171,16 @@ def test_pipelined_host_apply_matches_synchronous(ctx, prec):
         assert np.array_equal(y.numpy(), fac.apply(x, precision=prec))
 
 
-def test_autotune_keeps_results_and_never_slows_a_stage(ctx):
+@pytest.mark.parametrize("R", [16, 64])
+def test_autotune_keeps_results_and_never_slows_a_stage(ctx, R):
     """bfgFacAutotune re-deals chunks to CTAs; an item stays on one CTA with
-    its chunks in order, so the results are bit-identical."""
+    its chunks in order, so the results are bit-identical (16- and 32-RHS
+    tiles)."""
     g, fac = golden_fac("ellipse_n16384_k128", ctx)
-    X = torch.from_numpy(O.RefRng(50).complex_randn(16384 * 16).reshape(16384, 16)).cuda()
+    X = torch.from_numpy(O.RefRng(50).complex_randn(16384 * R).reshape(16384, R)).cuda()
     X = X.to(torch.complex64)
     y0 = fac.apply(X, precision="bf16x3")
-    times = fac.autotune("bf16x3", 16)
+    times = fac.autotune("bf16x3", R)
     assert times.shape[0] == len(fac.launch_info()) - 1          # stages, not the final sum
     assert np.all(times[:, 1] <= times[:, 0])
     assert torch.equal(fac.apply(X, precision="bf16x3"), y0)

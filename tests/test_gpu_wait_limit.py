@@ -18,7 +18,10 @@ pytestmark = pytest.mark.gpu
 import butterfly_gb300 as B  # noqa: E402
 
 
-def test_zero_wait_limit_times_out_and_the_factorization_recovers():
+@pytest.mark.parametrize("R", [16, 32])
+def test_zero_wait_limit_times_out_and_the_factorization_recovers(R):
+    """R = 16 runs the 16-RHS tile kernel, R = 32 the 32-RHS one (its own
+    warp roles: one MMA warp, eight extractor warps)."""
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     ctx = B.default_context(0)
@@ -26,7 +29,6 @@ def test_zero_wait_limit_times_out_and_the_factorization_recovers():
     fac = B.FacHelm2.make_multilevel(B.Helm2(float(g["k"])), B.Quadtree(g["src"]),
                                      B.Quadtree(g["tgt"]), context=ctx)
     n = fac.shape[1]
-    R = 16
     X = torch.from_numpy(B.Rng(21).complex_randn(n * R).reshape(n, R)).cuda().to(torch.complex64)
     lib = B.lib()
     Y = torch.empty_like(X)
