@@ -711,7 +711,7 @@ class _GmresResultC(ctypes.Structure):
                 ("converged", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
-PRECOND = {"none": 0, "block_jacobi": 1, "user": 2, "learned": 3}
+PRECOND = {"none": 0, "block_jacobi": 1, "user": 2, "learned": 3, "two_level": 4}
 _PRECOND_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                ctypes.c_void_p)
 
@@ -728,6 +728,9 @@ def _solver_sigs():
         "bfgSystemBuildBlockJacobi": [_VP],
         "bfgSystemApplyBlockJacobi": [_VP, _VP, _VP],
         "bfgSystemSetApplyPrecision": [_VP, ctypes.c_int32],
+        "bfgSystemBuildCoarse": [_VP, ctypes.c_int32, ctypes.POINTER(_I64)],
+        "bfgSystemCoarseMatrices": [_VP, _VP, _VP],
+        "bfgSystemApplyCoarse": [_VP, _VP, _VP],
         "bfgSolveGmres": [_VP, _VP, _VP, ctypes.c_double, _I64, ctypes.c_int32, _PRECOND_FN,
                           _VP, ctypes.POINTER(_GmresResultC)],
     }
@@ -813,13 +816,49 @@ class System:
                                                                  _VP(z.data_ptr())), "precond")
         return z
 
+    def build_coarse(self, extra_modes: int = 5) -> int:
+        """The two-level preconditioner's coarse space (bfgSystemBuildCoarse):
+        every curve's Fourier modes |m| <= ceil(k L / 2 pi) + extra_modes,
+        A_c = Phi^H A Phi and its inverse on the GPU.  Returns the coarse
+        dimension.  Use with solve_gmres(..., precond="two_level") after
+        build_block_jacobi()."""
+        import torch
+        d = _I64()
+        with self.ctx.on_stream(torch.cuda.current_stream().cuda_stream):
+            self._check(_solver_sigs().bfgSystemBuildCoarse(self.handle, int(extra_modes),
+                                                            ctypes.byref(d)), "coarse space")
+        self.coarse_dim = int(d.value)
+        return self.coarse_dim
+
+    def coarse_matrices(self):
+        """(A_c, A_c^-1) as device complex64 tensors (dim x dim)."""
+        import torch
+        D = self.coarse_dim
+        ac = torch.empty((D, D), dtype=torch.complex64, device="cuda")
+        ai = torch.empty_like(ac)
+        with self.ctx.on_stream(torch.cuda.current_stream().cuda_stream):
+            self._check(_solver_sigs().bfgSystemCoarseMatrices(self.handle, _VP(ac.data_ptr()),
+                                                               _VP(ai.data_ptr())), "coarse")
+        return ac, ai
+
+    def apply_coarse(self, r):
+        """z = Phi A_c^-1 Phi^H r (device complex128)."""
+        import torch
+        r = r.to(torch.complex128).contiguous()
+        z = torch.empty_like(r)
+        with self._stream(r):
+            self._check(_solver_sigs().bfgSystemApplyCoarse(self.handle, _VP(r.data_ptr()),
+                                                            _VP(z.data_ptr())), "coarse")
+        return z
+
 
 def solve_gmres(system: System, b, x0=None, tol: float = 1e-8, max_num_iter: int = None,
                 precond="block_jacobi"):
     """Right-preconditioned flexible GMRES on the GPU (bfSolveGMRES,
     linalg.c:47-317, with the preconditioner on the right).  ``precond``:
-    "none", "block_jacobi", or a callable (r_ptr, z_ptr, stream_ptr) -> None
-    applying z = M r to device complex128 vectors.  Returns (x, info)."""
+    "none", "block_jacobi", "learned", "two_level" (System.build_coarse), or
+    a callable (r_ptr, z_ptr, stream_ptr) -> None applying z = M r to device
+    complex128 vectors.  Returns (x, info)."""
     import torch
     L = _solver_sigs()
     b = b.to(torch.complex128).contiguous()

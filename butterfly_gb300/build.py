@@ -24,7 +24,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
           "-I" + os.path.join(ROOT, "include")]
 SOURCES = ["bfg_kernels.cu", "bfg_plan.cpp", "bfg_api.cpp", "bfg_noalloc.cu", "bfg_solver.cu",
            "bfg_tc.cu", "bfg_tree.cu", "bfg_df64.cu", "bfg_mlp.cu", "bfg_mlp_api.cpp",
-           "bfg_check.cpp", "bfg_sketch.cu"]
+           "bfg_check.cpp", "bfg_sketch.cu", "bfg_coarse.cu"]
 
 
 def nvcc() -> str:

@@ -32,6 +32,7 @@
 #include "../../include/bfg.h"
 #include "bfg_kernels.cuh"
 #include "bfg_mlp.cuh"
+#include "bfg_system.hpp"
 #include "hankel.cuh"
 
 namespace {
@@ -535,47 +536,10 @@ int gridFor(int64_t n, int t) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 32));
 }
 
-struct Dev {
-  void *p = nullptr;
-  size_t bytes = 0;
-  ~Dev() { if (p) cudaFree(p); }
-  cudaError_t alloc(size_t n) {
-    if (n <= bytes) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-    cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 16));
-    if (e == cudaSuccess) bytes = n;
-    return e;
-  }
-  template <typename T> T *as() const { return static_cast<T *>(p); }
-};
+using bfg::Dev;
 
 }  // namespace
 
-struct bfgSystem_s {
-  bfgContext ctx = nullptr;
-  bfgFac fac = nullptr;
-  int64_t n = 0, numCurves = 0;
-  int32_t order = 0;
-  double shift = 0.5;
-  bfgPrecision applyPrec = BFG_PRECISION_FP64;   // of the butterfly part
-  bfg::KernelParams kp{};
-  std::vector<int64_t> offsets;
-  Dev dOffsets, dCurveOf, dX, dW, dKrVal, dKrCol;
-  Dev tmpXw, tmpK;
-  // block-Jacobi
-  bool haveBj = false;
-  std::vector<int64_t> blkOff;
-  Dev dBlkOff, dInv, dInv32, dWork, dColBuf, dFlag;
-  // learned preconditioner: chunks of consecutive points of a curve
-  bfgMlp mlp = nullptr;
-  int32_t chunk = 0;
-  int64_t nChunks = 0;
-  Dev dChunkStart, dChunkLen, dFeat, dOut, dScale, dZbj;
-  std::string err;
-  cudaStream_t stream() const;
-};
 
 namespace {
 
@@ -632,6 +596,7 @@ bfgStatus bfgSystemCreate(bfgContext ctx, bfgFac fac, bfgHelm2 const *helm, doub
   sys->kp.betaRe = helm->betaRe;
   sys->kp.betaIm = helm->betaIm;
   sys->offsets.assign(curveOffsets, curveOffsets + numCurves + 1);
+  sys->weights.assign(weights, weights + sys->offsets.back());
   cudaStream_t s = sys->stream();
   std::vector<int64_t> curveOf(n);
   for (int64_t b = 0; b < numCurves; ++b)
@@ -794,6 +759,22 @@ void applyBj32(bfgSystem sys, double2 const *r, double2 *z, cudaStream_t s) {
 }
 }  // namespace
 
+}  // extern "C"
+
+namespace bfg {
+bfgStatus systemApplyPrec(bfgSystem sys, bfgPrecision prec, void const *X, void *Y) {
+  return systemApply(sys, prec, X, Y);
+}
+void applyBlockJacobi32(bfgSystem sys, double2 const *r, double2 *z, cudaStream_t s) {
+  applyBj32(sys, r, z, s);
+}
+void launchSubFrom(int64_t n, double2 const *x, double2 *y, cudaStream_t s) {
+  subFromKernel<<<gridFor(n, 256), 256, 0, s>>>(n, x, y);
+}
+}  // namespace bfg
+
+extern "C" {
+
 bfgStatus bfgSystemSetLearnedPreconditioner(bfgSystem sys, bfgMlp mlp, int32_t chunk) {
   if (!sys || !mlp || chunk < 1) return BFG_ERROR_INVALID_ARGUMENTS;
   if (!sys->haveBj) return sysFail(sys, BFG_ERROR_INVALID_ARGUMENTS, "learned: block-Jacobi not built");
@@ -860,8 +841,12 @@ bfgStatus bfgSolveGmres(bfgSystem sys, void const *B, void *X, double tol, int64
     return sysFail(sys, BFG_ERROR_INVALID_ARGUMENTS, "user preconditioner missing");
   if (precond == BFG_PRECOND_LEARNED && !sys->mlp)
     return sysFail(sys, BFG_ERROR_INVALID_ARGUMENTS, "learned preconditioner not set");
+  if (precond == BFG_PRECOND_TWO_LEVEL && !(sys->haveCoarse && sys->haveBj))
+    return sysFail(sys, BFG_ERROR_INVALID_ARGUMENTS,
+                   "two-level preconditioner: block-Jacobi and the coarse space not built");
   if (precond != BFG_PRECOND_NONE && precond != BFG_PRECOND_BLOCK_JACOBI &&
-      precond != BFG_PRECOND_USER && precond != BFG_PRECOND_LEARNED)
+      precond != BFG_PRECOND_USER && precond != BFG_PRECOND_LEARNED &&
+      precond != BFG_PRECOND_TWO_LEVEL)
     return sysFail(sys, BFG_ERROR_INVALID_ARGUMENTS, "unknown preconditioner");
   auto t0 = std::chrono::steady_clock::now();
   cudaStream_t s = sys->stream();
@@ -910,6 +895,7 @@ bfgStatus bfgSolveGmres(bfgSystem sys, void const *B, void *X, double tol, int64
       SYS_CK(cudaGetLastError());
       return BFG_OK;
     }
+    if (precond == BFG_PRECOND_TWO_LEVEL) return bfg::applyTwoLevel(sys, in, outv);
     if (precond == BFG_PRECOND_LEARNED) {
       applyBj32(sys, in, outv, s);
       int64_t const *cs = sys->dChunkStart.as<int64_t>();

@@ -368,6 +368,30 @@ bfgStatus bfgSystemApplyBlockJacobi(bfgSystem sys, void const *R, void *Z);
 #define BFG_PRECOND_BLOCK_JACOBI 1
 #define BFG_PRECOND_USER 2
 #define BFG_PRECOND_LEARNED 3
+#define BFG_PRECOND_TWO_LEVEL 4
+
+/* ---- Two-level preconditioner (a GB300 addition; the reference
+ * preconditions with block-Jacobi only) ----
+ * A coarse space of every curve's discrete Fourier modes: with the points
+ * j = 0 .. n_b - 1 of curve b equispaced in its parameter (as the
+ * reference's circles are, ellipse.c), Phi_b[j, m] = e^{i mu 2 pi j / n_b} /
+ * sqrt(n_b) for mu = -q_b .. q_b, q_b = min(ceil(k L_b / 2 pi) + extraModes,
+ * (n_b - 1) / 2) with L_b the sum of the curve's quadrature weights (its
+ * length: the modes that radiate, plus extraModes).  Builds A_c = Phi^H A
+ * Phi from one apply of the system to all coarse basis vectors (butterfly
+ * part in split-BF16 on the tensor cores) and inverts it by block
+ * Gauss-Jordan elimination over the curves' mode blocks (pivoting inside a
+ * block), in FP32; at most 128 modes per curve.  With
+ * BFG_PRECOND_TWO_LEVEL, bfgSolveGmres applies the multiplicative
+ * two-level preconditioner z1 = Phi A_c^-1 Phi^H r, z = z1 + M_bj (r - A z1)
+ * (block-Jacobi built; the system apply in the iterations' precision).
+ * *dim: the coarse dimension (may be NULL). */
+bfgStatus bfgSystemBuildCoarse(bfgSystem sys, int32_t extraModes, int64_t *dim);
+/* A_c and A_c^-1 (device complex64, dim x dim row-major; either may be
+ * NULL). */
+bfgStatus bfgSystemCoarseMatrices(bfgSystem sys, void *Ac, void *AcInv);
+/* z = Phi A_c^-1 Phi^H r (device complex128 vectors). */
+bfgStatus bfgSystemApplyCoarse(bfgSystem sys, void const *R, void *Z);
 
 /* ---- Learned preconditioner (a GB300 addition; the reference
  * preconditions with block-Jacobi only) ---- */

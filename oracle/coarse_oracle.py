@@ -12,7 +12,9 @@ radiate), carries most of that coupling:
   additive:        z = M_bj r + Phi A_c^-1 Phi^H r
   multiplicative:  z1 = Phi A_c^-1 Phi^H r,  z = z1 + M_bj (r - A z1)
 
-with A_c = Phi^H A Phi.  The solver is right-preconditioned flexible GMRES
+with A_c = Phi^H A Phi, inverted by block Gauss-Jordan elimination over the
+circles' mode blocks (block_gauss_jordan, the GPU's algorithm).  The solver
+is right-preconditioned flexible GMRES
 (the method's FGMRES, linalg.c:47-317 with the preconditioner on the right)
 with classical Gram-Schmidt and a second orthogonalisation pass.
 """
@@ -84,6 +86,40 @@ def block_jacobi(A, offsets):
     return apply
 
 
+def mode_counts_from_weights(weights, offsets, k, extra=0):
+    """Modes |m| <= q_b per curve from its quadrature weights: q_b =
+    min(ceil(k L_b / 2 pi) + extra, (n_b - 1) / 2), L_b = sum of the curve's
+    weights (its length: 2 pi r for a circle, so q_b = ceil(k r) + extra),
+    as bfgSystemBuildCoarse counts them."""
+    q = []
+    for b in range(len(offsets) - 1):
+        nb = int(offsets[b + 1] - offsets[b])
+        L = float(np.sum(weights[offsets[b]:offsets[b + 1]]))
+        q.append(max(0, min(int(math.ceil(k * L / (2.0 * math.pi))) + extra, (nb - 1) // 2)))
+    return q
+
+
+def block_gauss_jordan(A, starts):
+    """The inverse of A by block Gauss-Jordan elimination with the diagonal
+    blocks [starts[b], starts[b+1]) as pivots in order (partial pivoting only
+    inside a block's own inverse), as the GPU inverts A_c: for block K and
+    the rest O,
+      P = A_KK^-1;  A_KO <- P A_KO;  A_OO <- A_OO - A_OK A_KO;
+      A_OK <- -A_OK P;  A_KK <- P."""
+    A = np.array(A, dtype=complex)
+    for b in range(len(starts) - 1):
+        K = slice(int(starts[b]), int(starts[b + 1]))
+        P = np.linalg.inv(A[K, K])
+        T = P @ A[K, :]
+        U = A[:, K].copy()
+        U[K, :] = 0
+        A -= U @ T
+        A[:, K] = -U @ P
+        A[K, :] = T
+        A[K, K] = P
+    return A
+
+
 class FourierCoarse:
     """The per-circle Fourier coarse space and its exact coarse solve.
 
@@ -91,12 +127,13 @@ class FourierCoarse:
     circle sampled at equispaced angles 2 pi j / n_b, as scattering_geometry
     places them); modes per circle |m| <= min(ceil(k r) + extra, (n_b-1)/2)."""
 
-    def __init__(self, A, offsets, circles, k, extra=0):
+    def __init__(self, A, offsets, circles, k, extra=0, modes=None):
         self.offsets = np.asarray(offsets)
         self.bases, start = [], [0]
         for b in range(len(offsets) - 1):
             nb = int(offsets[b + 1] - offsets[b])
-            q = min(int(math.ceil(k * circles[b][2])) + extra, (nb - 1) // 2)
+            q = modes[b] if modes is not None else \
+                min(int(math.ceil(k * circles[b][2])) + extra, (nb - 1) // 2)
             th = 2.0 * np.pi * np.arange(nb) / nb
             self.bases.append(np.exp(1j * np.outer(th, np.arange(-q, q + 1))) / math.sqrt(nb))
             start.append(start[-1] + 2 * q + 1)

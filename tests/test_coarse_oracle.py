@@ -51,3 +51,26 @@ def test_fourier_coarse_space_cuts_iterations(system):
     assert res_add < 1e-8 and res_mul < 1e-8
     assert it_add * 2 <= it_bj                  # measured 29 against 79
     assert it_mul * 6 <= it_bj                  # measured 8
+
+
+def test_block_gauss_jordan_inverts_the_coarse_operator(system):
+    """The GPU's algorithm for A_c^-1: block pivots on the circles' mode
+    blocks, no pivoting across blocks.  On the coarse operator of the CFIE
+    it agrees with LAPACK's inverse to rounding."""
+    A, b, off, circles = system
+    w = np.concatenate([np.full(int(off[i + 1] - off[i]), 2 * np.pi * circles[i][2] /
+                                (off[i + 1] - off[i])) for i in range(len(off) - 1)])
+    q = C.mode_counts_from_weights(w, off, K, extra=5)
+    assert q == [min(int(np.ceil(K * c[2])) + 5, (int(off[i + 1] - off[i]) - 1) // 2)
+                 for i, c in enumerate(circles)]
+    coarse = C.FourierCoarse(A, off, circles, K, modes=q)
+    Ainv = C.block_gauss_jordan(coarse.Ac, coarse.start)
+    ref = np.linalg.inv(coarse.Ac)
+    assert np.linalg.norm(Ainv - ref) / np.linalg.norm(ref) < 1e-10
+    # and on a matrix that needs row exchanges inside a block
+    rng = np.random.default_rng(3)
+    M = rng.standard_normal((12, 12)) + 1j * rng.standard_normal((12, 12))
+    M[:4, :4] = 6 * np.fliplr(np.eye(4))      # zero diagonal: block 0 needs row exchanges
+    M += 8 * np.eye(12) * (np.arange(12) >= 4)
+    Minv = C.block_gauss_jordan(M, [0, 4, 8, 12])
+    assert np.linalg.norm(Minv @ M - np.eye(12)) < 1e-10
