@@ -61,15 +61,15 @@ NCU_DRAM_PER_ALG = {("c2", "fp32", 16): [0.7973, 1.0266, 0.9855, 0.7925],
                     ("c2", "bf16x3", 16): [0.8888, 1.0627, 1.0246, 1.0386],
                     ("c2s", "fp32", 16): [0.7973, 1.0266, 0.9855, 0.7925],
                     ("c2s", "bf16x3", 16): [0.8888, 1.0627, 1.0246, 1.0386],
-                    ("c2", "bf16x3", 256): [0.536],
-                    ("c4", "bf16x3", 256): [0.536]}
+                    ("c2", "bf16x3", 256): [0.537, 1.055],
+                    ("c4", "bf16x3", 256): [0.537, 1.055]}
 NCU_TRAFFIC_SOURCE = {
     ("c2", 16): "ncu DRAM bytes of the same stage in a capture of the 32,768-point workload, "
                 "scaled by algorithmic bytes",
     ("c2s", 16): "ncu capture",
-    ("c2", 256): "ncu capture (stage 0 of the 65,536-point workload at 256 RHS)",
+    ("c2", 256): "ncu capture (stages 0 and 1 of the 65,536-point workload at 256 RHS)",
     ("c4", 256): "ncu DRAM bytes per algorithmic byte of the same stage in a capture of the "
-                 "65,536-point workload at 256 RHS (stage 0), times this launch's "
+                 "65,536-point workload at 256 RHS (stages 0 and 1), times this launch's "
                  "algorithmic bytes"}
 ERR_BOUND = 1e-6
 

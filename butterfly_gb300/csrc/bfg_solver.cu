@@ -403,6 +403,92 @@ __global__ void learnedApplyKernel(int chunk, int64_t const *start, int32_t cons
   }
 }
 
+// The same inversion in FP32 and in place (the preconditioner of the
+// iterations needs no more): Gauss-Jordan with partial pivoting, a_kk <-
+// 1 / pivot, column k <- -a_ik / pivot, the row exchanges undone on the
+// columns at the end (perm: one int per row of the block).
+__global__ void __launch_bounds__(1024) gaussJordan32Kernel(int64_t const *offsets,
+                                                            int64_t const *blkOff, float2 *A,
+                                                            int32_t *permBuf, float2 *colBuf,
+                                                            int32_t *singular) {
+  int64_t const b = blockIdx.x;
+  int64_t const m = offsets[b + 1] - offsets[b];
+  float2 *a = A + blkOff[b];
+  int32_t *perm = permBuf + offsets[b];
+  float2 *colk = colBuf + offsets[b];
+  __shared__ float red[32];
+  __shared__ int64_t redIdx[32];
+  __shared__ int64_t sPiv;
+  int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int64_t k = 0; k < m; ++k) {
+    float best = -1.f;
+    int64_t bi = k;
+    for (int64_t r = k + threadIdx.x; r < m; r += blockDim.x) {
+      float2 const z = a[r * m + k];
+      float const mag = z.x * z.x + z.y * z.y;
+      if (mag > best) { best = mag; bi = r; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      float const ob = __shfl_xor_sync(0xffffffffu, best, o);
+      int64_t const oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    if (lane == 0) { red[warp] = best; redIdx[warp] = bi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float bb = -1.f;
+      int64_t ii = k;
+      for (int q = 0; q < nw; ++q)
+        if (red[q] > bb || (red[q] == bb && redIdx[q] < ii)) { bb = red[q]; ii = redIdx[q]; }
+      sPiv = ii;
+      perm[k] = (int32_t)ii;
+      if (!(bb > 0.f)) atomicOr(singular, 1);
+    }
+    __syncthreads();
+    int64_t const piv = sPiv;
+    if (piv != k)
+      for (int64_t c = threadIdx.x; c < m; c += blockDim.x) {
+        float2 const t = a[k * m + c]; a[k * m + c] = a[piv * m + c]; a[piv * m + c] = t;
+      }
+    __syncthreads();
+    float2 const d = a[k * m + k];
+    float const dd = d.x * d.x + d.y * d.y;
+    float2 const dinv = dd > 0.f ? make_float2(d.x / dd, -d.y / dd) : make_float2(0.f, 0.f);
+    __syncthreads();
+    for (int64_t c = threadIdx.x; c < m; c += blockDim.x) {
+      float2 const v = a[k * m + c];
+      a[k * m + c] = c == k ? dinv : make_float2(v.x * dinv.x - v.y * dinv.y,
+                                                 v.x * dinv.y + v.y * dinv.x);
+    }
+    for (int64_t r = threadIdx.x; r < m; r += blockDim.x) colk[r] = a[r * m + k];
+    __syncthreads();
+    for (int64_t e = threadIdx.x; e < m * m; e += blockDim.x) {
+      int64_t const r = e / m, c = e % m;
+      if (r == k || c == k) continue;
+      float2 const f = colk[r], ak = a[k * m + c];
+      float2 v = a[e];
+      v.x -= f.x * ak.x - f.y * ak.y;
+      v.y -= f.x * ak.y + f.y * ak.x;
+      a[e] = v;
+    }
+    __syncthreads();
+    for (int64_t r = threadIdx.x; r < m; r += blockDim.x)
+      if (r != k) {
+        float2 const f = colk[r];
+        a[r * m + k] = make_float2(-(f.x * dinv.x - f.y * dinv.y), -(f.x * dinv.y + f.y * dinv.x));
+      }
+    __syncthreads();
+  }
+  for (int64_t k = m - 1; k >= 0; --k) {
+    int64_t const p = perm[k];
+    if (p != k)
+      for (int64_t r = threadIdx.x; r < m; r += blockDim.x) {
+        float2 const t = a[r * m + k]; a[r * m + k] = a[r * m + p]; a[r * m + p] = t;
+      }
+    __syncthreads();
+  }
+}
+
 __global__ void c128ToC64FlatKernel(int64_t n, double2 const *a, float2 *b) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -701,8 +787,9 @@ bfgStatus bfgSystemBuildBlockJacobi(bfgSystem sys) {
   int64_t const tot = sys->blkOff[nb];
   SYS_CK(sys->dBlkOff.alloc((nb + 1) * 8));
   SYS_CK(sys->dWork.alloc(tot * 16));
-  SYS_CK(sys->dInv.alloc(tot * 16));
+  SYS_CK(sys->dInv32.alloc(tot * 8));
   SYS_CK(sys->dColBuf.alloc(sys->n * 16));
+  SYS_CK(sys->dPerm.alloc(sys->n * 4));
   SYS_CK(sys->dFlag.alloc(4));
   SYS_CK(cudaMemcpyAsync(sys->dBlkOff.p, sys->blkOff.data(), (nb + 1) * 8, cudaMemcpyHostToDevice, s));
   SYS_CK(cudaMemsetAsync(sys->dFlag.p, 0, 4, s));
@@ -720,20 +807,20 @@ bfgStatus bfgSystemBuildBlockJacobi(bfgSystem sys) {
       sys->dKrCol.as<int64_t>(), 2 * sys->order, sys->dW.as<double>(), sys->shift,
       sys->dWork.as<double2>());
   SYS_CK(cudaGetLastError());
-  gaussJordanKernel<<<(unsigned)nb, 512, 0, s>>>(sys->dOffsets.as<int64_t>(),
-                                                  sys->dBlkOff.as<int64_t>(),
-                                                  sys->dWork.as<double2>(), sys->dInv.as<double2>(),
-                                                  sys->dColBuf.as<double2>(), sys->dFlag.as<int32_t>());
+  // the FP32 inverses for the iterations, inverted in place in FP32; the
+  // FP64 blocks stay for the FP64 inverses, formed on the first FP64 apply
+  c128ToC64FlatKernel<<<gridFor(tot, 256), 256, 0, s>>>(tot, sys->dWork.as<double2>(),
+                                                        sys->dInv32.as<float2>());
+  gaussJordan32Kernel<<<(unsigned)nb, 1024, 0, s>>>(
+      sys->dOffsets.as<int64_t>(), sys->dBlkOff.as<int64_t>(), sys->dInv32.as<float2>(),
+      sys->dPerm.as<int32_t>(), reinterpret_cast<float2 *>(sys->dColBuf.p), sys->dFlag.as<int32_t>());
   SYS_CK(cudaGetLastError());
   int32_t flag = 0;
   SYS_CK(cudaMemcpyAsync(&flag, sys->dFlag.p, 4, cudaMemcpyDeviceToHost, s));
   SYS_CK(cudaStreamSynchronize(s));
   if (flag) return sysFail(sys, BFG_ERROR_NUMERICAL, "block-Jacobi: a diagonal block is singular");
-  SYS_CK(sys->dInv32.alloc(tot * 8));
-  c128ToC64FlatKernel<<<gridFor(tot, 256), 256, 0, s>>>(tot, sys->dInv.as<double2>(),
-                                                        sys->dInv32.as<float2>());
-  SYS_CK(cudaGetLastError());
   sys->haveBj = true;
+  sys->haveBj64 = false;
   return BFG_OK;
 }
 
@@ -742,6 +829,21 @@ bfgStatus bfgSystemApplyBlockJacobi(bfgSystem sys, void const *R, void *Z) {
   if (!sys->haveBj) return sysFail(sys, BFG_ERROR_INVALID_ARGUMENTS, "block-Jacobi not built");
   cudaStream_t s = sys->stream();
   int64_t const n = sys->n;
+  if (!sys->haveBj64) {
+    // the FP64 inverses, on first use (the FP64 blocks are consumed)
+    int64_t const tot = sys->blkOff[sys->numCurves];
+    SYS_CK(sys->dInv.alloc(tot * 16));
+    SYS_CK(cudaMemsetAsync(sys->dFlag.p, 0, 4, s));
+    gaussJordanKernel<<<(unsigned)sys->numCurves, 512, 0, s>>>(
+        sys->dOffsets.as<int64_t>(), sys->dBlkOff.as<int64_t>(), sys->dWork.as<double2>(),
+        sys->dInv.as<double2>(), sys->dColBuf.as<double2>(), sys->dFlag.as<int32_t>());
+    SYS_CK(cudaGetLastError());
+    int32_t flag = 0;
+    SYS_CK(cudaMemcpyAsync(&flag, sys->dFlag.p, 4, cudaMemcpyDeviceToHost, s));
+    SYS_CK(cudaStreamSynchronize(s));
+    if (flag) return sysFail(sys, BFG_ERROR_NUMERICAL, "block-Jacobi: a diagonal block is singular");
+    sys->haveBj64 = true;
+  }
   blockDiagApplyKernel<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(
       n, sys->dCurveOf.as<int64_t>(), sys->dOffsets.as<int64_t>(), sys->dBlkOff.as<int64_t>(),
       sys->dInv.as<double2>(), static_cast<double2 const *>(R), static_cast<double2 *>(Z));

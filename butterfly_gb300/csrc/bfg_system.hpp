@@ -55,9 +55,9 @@ struct bfgSystem_s {
   Dev dOffsets, dCurveOf, dX, dW, dKrVal, dKrCol;
   Dev tmpXw, tmpK;
   // block-Jacobi
-  bool haveBj = false;
+  bool haveBj = false, haveBj64 = false;   // the FP32 inverses; the FP64 ones (on first use)
   std::vector<int64_t> blkOff;
-  Dev dBlkOff, dInv, dInv32, dWork, dColBuf, dFlag;
+  Dev dBlkOff, dInv, dInv32, dWork, dColBuf, dPerm, dFlag;
   // learned preconditioner: chunks of consecutive points of a curve
   bfgMlp mlp = nullptr;
   int32_t chunk = 0;
