@@ -284,7 +284,9 @@ constexpr int32_t kSketchMinRank = 128;
 // the triangular factor of a QR of Z_equiv, which converges in fewer sweeps
 // than the one-sided Jacobi on Z_equiv itself (factorization time at
 // 65,536 / 262,144 points and of the 256-problem batch: 1.95 -> 1.12 s,
-// 34.7 -> 24.2 s, 48.3 -> 26.1 s; the same operators to rounding)
+// 34.7 -> 24.2 s, 48.3 -> 26.1 s; the same operators to rounding).  The
+// random Q stays at full width: with Q = I the QR of Z_equiv^H is not rank
+// revealing and the sweeps were slower again (24.2 -> 31.0 s)
 constexpr int32_t kQrMinRank = 32;
 constexpr double kSketchMaxFraction = 0.8;
 constexpr double kSketchWidthScale = 1.1;
