@@ -507,17 +507,15 @@ bfgStatus bfgSystemBuildCoarse(bfgSystem sys, int32_t extraModes, int64_t *dimOu
   // A_c = Phi^H Y, curve by curve
   CO_CK(sys->dAc.alloc((size_t)D * D * 8));
   std::vector<CGemm> g((size_t)nb);
-  int maxN = 0;
   for (int64_t b = 0; b < nb; ++b) {
     int const M = (int)(sys->cStart[b + 1] - sys->cStart[b]);
     int64_t const nbp = sys->offsets[b + 1] - sys->offsets[b];
     g[b] = CGemm{sys->dTab.as<float2>() + sys->tabOff[b], ky.as<float2>() + sys->offsets[b] * D,
                  sys->dAc.as<float2>() + sys->cStart[b] * D, M, D, D, M, (int32_t)D,
                  (int32_t)nbp, 1, 1.f, 0.f};
-    maxN = (int)D;
   }
   Dev dDesc;
-  CO_CK(runGemm(g.data(), (int)nb, maxM, maxN, dDesc, s));
+  CO_CK(runGemm(g.data(), (int)nb, maxM, (int)D, dDesc, s));
   CO_CK(cudaStreamSynchronize(s));
   xw.release();
   ky.release();
