@@ -1170,6 +1170,11 @@ def main():
                "sample": "the reference's apply algorithm (oracle C port) over this "
                          "factorization's structure with stand-in values, %d of %d RHS, "
                          "median of 3" % (Rs, R)}
+        # the same on one core (the reference's own apply is single-threaded
+        # apart from its BLAS calls)
+        v1, Rs1, _ = cpu_port_time(plan_text, Xh, 1, budget_s=12.0)
+        cpu["one_thread"] = {"value": v1, "unit": "RHS/s", "cores": 1,
+                             "sample": "%d of %d RHS, median of 3" % (Rs1, R)}
     c2 = None
     if world == 1 and not args.no_c2 and args.config != "c2":
         try:
