@@ -77,6 +77,7 @@ struct GemmDesc {
   double const *rowScale;   // optional: row i of C scaled by rowScale[i]
   int64_t lda, ldb, ldc;
   int32_t M, N, K, opA;     // opA 0: A is M x K; 1: C = A^H B with A stored K x M
+  double const *colScale;   // optional: column j of C scaled by colScale[j]
 };
 
 struct HqrDesc {
@@ -275,8 +276,10 @@ __global__ void __launch_bounds__(256) zgemmKernel(GemmDesc const *__restrict__ 
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
       int const gj = j0 + tx + 16 * c;
-      if (gj < g.N)
-        g.C[gi + (int64_t)gj * g.ldc] = make_double2(sc * acc[r][c].x, sc * acc[r][c].y);
+      if (gj < g.N) {
+        double const scc = g.colScale ? sc * g.colScale[gj] : sc;
+        g.C[gi + (int64_t)gj * g.ldc] = make_double2(scc * acc[r][c].x, scc * acc[r][c].y);
+      }
     }
   }
 }
@@ -918,8 +921,13 @@ cudaError_t runSketchReexpansion(std::vector<SketchInput> const &in, PointsDev s
       return err;
     if ((err = cudaStreamSynchronize(s)) != cudaSuccess) return err;
 
-    // accepted groups: X = Q2 (W (diag(w) (T^H (Q^H Z_orig)))) per member
-    std::vector<GemmDesc> gc, gd, ge, gx;
+    // accepted groups: X = Q2 (W (diag(w) (T^H (Q^H Z_orig)))) per member.
+    // A group whose members have more columns in all than Z_equiv has rows
+    // forms E = Q2 W and F^H = Q T diag(w) once (in the free Z and G
+    // buffers), and each member then takes X = E (F Z_orig): two products
+    // per member instead of four
+    std::vector<GemmDesc> gc, gd, ge, gx, gE, gF;
+    std::vector<char> fused(nb, 0);
     std::vector<Group> requeue;
     for (size_t i = 0; i < nb; ++i) {
       SketchDev const &b = blks[i];
@@ -938,6 +946,16 @@ cudaError_t runSketchReexpansion(std::vector<SketchInput> const &in, PointsDev s
         continue;
       }
       rep->groups += 1;
+      int64_t sumN = 0;
+      for (auto const &d : gr.mem) sumN += d.n;
+      if (sumN > b.p) {
+        fused[i] = 1;
+        double const *w = reinterpret_cast<double const *>(S + b.oSW) + b.l;
+        gE.push_back(GemmDesc{S + b.oB2, S + b.oM + b.l, S + b.oZ, nullptr, b.p, 2 * b.l, b.p, b.p,
+                              b.l, b.l, 0, nullptr});
+        gF.push_back(GemmDesc{S + b.oB0, S + b.oM, S + b.oB1, nullptr, b.p, 2 * b.l, b.p, b.p, b.l,
+                              b.l, 0, w});
+      }
     }
     for (size_t mi = 0; mi < mems.size(); ++mi) {
       size_t const i = memberOf[mi];
@@ -945,17 +963,29 @@ cudaError_t runSketchReexpansion(std::vector<SketchInput> const &in, PointsDev s
       if (failed[i] && b.l < b.p) continue;
       SketchDev const &m = mems[mi];
       double const *w = reinterpret_cast<double const *>(S + b.oSW) + b.l;
-      gc.push_back(GemmDesc{S + b.oB0, S + m.oZo, S + m.oC, nullptr, b.p, b.p, b.l, b.l, m.n, b.p, 1});
-      gd.push_back(GemmDesc{S + b.oM, S + m.oC, S + m.oD, w, 2 * b.l, b.l, b.l, b.l, m.n, b.l, 1});
-      ge.push_back(GemmDesc{S + b.oM + b.l, S + m.oD, S + m.oC, nullptr, 2 * b.l, b.l, b.l, b.l,
-                            m.n, b.l, 0});
-      gx.push_back(GemmDesc{S + b.oB2, S + m.oC, arena + m.arenaOff, nullptr, b.p, b.l, b.p, b.p,
-                            m.n, b.l, 0});
+      if (fused[i]) {
+        // Y1 = F Z_orig = (F^H)^H Z_orig into C, X = E Y1
+        gc.push_back(GemmDesc{S + b.oB1, S + m.oZo, S + m.oC, nullptr, b.p, b.p, b.l, b.l, m.n,
+                              b.p, 1, nullptr});
+        gx.push_back(GemmDesc{S + b.oZ, S + m.oC, arena + m.arenaOff, nullptr, b.p, b.l, b.p, b.p,
+                              m.n, b.l, 0, nullptr});
+      } else {
+        gc.push_back(GemmDesc{S + b.oB0, S + m.oZo, S + m.oC, nullptr, b.p, b.p, b.l, b.l, m.n,
+                              b.p, 1, nullptr});
+        gd.push_back(GemmDesc{S + b.oM, S + m.oC, S + m.oD, w, 2 * b.l, b.l, b.l, b.l, m.n, b.l, 1,
+                              nullptr});
+        ge.push_back(GemmDesc{S + b.oM + b.l, S + m.oD, S + m.oC, nullptr, 2 * b.l, b.l, b.l, b.l,
+                              m.n, b.l, 0, nullptr});
+        gx.push_back(GemmDesc{S + b.oB2, S + m.oC, arena + m.arenaOff, nullptr, b.p, b.l, b.p, b.p,
+                              m.n, b.l, 0, nullptr});
+      }
       ++rep->blocks;
       rep->maxWidth = std::max<int64_t>(rep->maxWidth, b.l);
       rep->sumWidth += b.l;
     }
     mark(7);
+    if ((err = launchGemms(gE, dDesc, dTiles, s)) != cudaSuccess) return err;
+    if ((err = launchGemms(gF, dDesc, dTiles, s)) != cudaSuccess) return err;
     if ((err = launchGemms(gc, dDesc, dTiles, s)) != cudaSuccess) return err;
     if ((err = launchGemms(gd, dDesc, dTiles, s)) != cudaSuccess) return err;
     if ((err = launchGemms(ge, dDesc, dTiles, s)) != cudaSuccess) return err;
