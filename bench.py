@@ -1136,6 +1136,20 @@ def main():
         if pipelined:
             ctx.check(lib.bfgFacApplyHostWait(fac.handle))
 
+    # the raw host<->device copy times of one step's operands, for reading
+    # the end-to-end figure against
+    dcopy = torch.empty((n, R), dtype=torch.complex128, device="cuda")
+    copy_ms = {}
+    for name, fn in (("h2d", lambda: dcopy.copy_(Xp[0], non_blocking=True)),
+                     ("d2h", lambda: Yp[0].copy_(dcopy, non_blocking=True))):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        copy_ms[name] = (time.perf_counter() - t0) / 3 * 1e3
+    del dcopy
     e2e_t = {}
     for pipelined in (True, False):
         host_steps(2, pipelined)
@@ -1147,7 +1161,8 @@ def main():
            "h2d_bytes_per_step": n * R * 16, "d2h_bytes_per_step": n * R * 16,
            "precision": head, "call": "bfgFacApplyHostAsync (pipelined), one wait",
            "steps": e2e_steps,
-           "synchronous_call_value": world * R * e2e_steps / e2e_t[False]}
+           "synchronous_call_value": world * R * e2e_steps / e2e_t[False],
+           "copy_ms": copy_ms}
     del Xp, Yp
 
     # one right-hand side: the HBM-bound single-vector apply
