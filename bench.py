@@ -109,6 +109,40 @@ def factorization_work(table, st):
             "reference_equivalent_tflops": svd / reexp_s / 1e12 if reexp_s > 0 else None}
 
 
+def gpu_local_cpus(dev=0):
+    """The host CPUs of the NUMA node the GPU's PCI device reports, or None
+    (one node, or nothing reported)."""
+    try:
+        import torch
+        pr = torch.cuda.get_device_properties(dev)
+        addr = "%04x:%02x:%02x.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+        node = int(open("/sys/bus/pci/devices/%s/numa_node" % addr).read())
+        if node < 0:
+            return None
+        cpus = set()
+        for part in open("/sys/devices/system/node/node%d/cpulist" % node).read().strip().split(","):
+            a, _, b = part.partition("-")
+            cpus.update(range(int(a), int(b or a) + 1))
+        return cpus & os.sched_getaffinity(0) or None
+    except Exception:
+        return None
+
+
+def pinned_local(make):
+    """make() run with the calling thread on the GPU's NUMA node, so that the
+    pinned host pages it first touches sit next to the GPU; (result, node
+    CPUs or None)."""
+    cpus = gpu_local_cpus()
+    if not cpus:
+        return make(), None
+    old = os.sched_getaffinity(0)
+    try:
+        os.sched_setaffinity(0, cpus)
+        return make(), sorted(cpus)
+    finally:
+        os.sched_setaffinity(0, old)
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1121,8 +1155,9 @@ def main():
     # step's compute) with one wait at the end, and the synchronous call
     # (bfgFacApplyHost) timed beside it
     e2e_steps = steps_p[head]
-    Xp = [torch.from_numpy(Xh).pin_memory() for _ in range(2)]
-    Yp = [torch.empty((n, R), dtype=torch.complex128).pin_memory() for _ in range(2)]
+    (Xp, Yp), local_cpus = pinned_local(lambda: (
+        [torch.from_numpy(Xh).pin_memory() for _ in range(2)],
+        [torch.zeros((n, R), dtype=torch.complex128).pin_memory() for _ in range(2)]))
     lib = B.lib()
     P = B.PRECISIONS[head]
 
@@ -1141,7 +1176,9 @@ def main():
     dcopy = torch.empty((n, R), dtype=torch.complex128, device="cuda")
     copy_ms = {}
     for name, fn in (("h2d", lambda: dcopy.copy_(Xp[0], non_blocking=True)),
-                     ("d2h", lambda: Yp[0].copy_(dcopy, non_blocking=True))):
+                     ("h2d_second_buffer", lambda: dcopy.copy_(Xp[1], non_blocking=True)),
+                     ("d2h", lambda: Yp[0].copy_(dcopy, non_blocking=True)),
+                     ("d2h_second_buffer", lambda: Yp[1].copy_(dcopy, non_blocking=True))):
         fn()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -1162,7 +1199,8 @@ def main():
            "precision": head, "call": "bfgFacApplyHostAsync (pipelined), one wait",
            "steps": e2e_steps,
            "synchronous_call_value": world * R * e2e_steps / e2e_t[False],
-           "copy_ms": copy_ms}
+           "copy_ms": copy_ms,
+           "pinned_on_gpu_node_cpus": len(local_cpus) if local_cpus else None}
     del Xp, Yp
 
     # one right-hand side: the HBM-bound single-vector apply
