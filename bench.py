@@ -1089,12 +1089,13 @@ def main():
         Y16 = torch.empty((n, R), dtype=torch.complex64, device="cuda")
         Ydf = torch.empty_like(Y64)
     stream.synchronize()
-    # the tensor-core schedules: per stage the fastest of several CTA dealings
-    # (bfgFacAutotune), before anything is timed
+    # the tensor-core schedules: the RHS tile width and per stage the fastest
+    # of several CTA dealings (bfgFacAutotune), before anything is timed
     tuned = {}
     for p in ("bf16x3", "bf16x2"):
         t = fac.autotune(p, R)
-        tuned[p] = {"default_ms": [float(v) for v in t[:, 0]], "tuned_ms": [float(v) for v in t[:, 1]]}
+        tuned[p] = {"default_ms": [float(v) for v in t[:, 0]], "tuned_ms": [float(v) for v in t[:, 1]],
+                    "rhs_tile": fac.rhs_tile(p, R)}
     precs = {"fp64": (X64, Y64), "df64": (X64, Ydf), "fp32": (X32, Y32), "bf16x3": (X32, Y16),
              "bf16x2": (X32, Y16)}
     outs = {}

@@ -140,6 +140,7 @@ def lib() -> ctypes.CDLL:
         "bfgFacPrepare": [_VP, ctypes.c_int32],
         "bfgFacAutotune": [_VP, ctypes.c_int32, _I64, _VP, ctypes.c_int32,
                            ctypes.POINTER(ctypes.c_int32)],
+        "bfgFacGetRhsTile": [_VP, ctypes.c_int32, _I64, ctypes.POINTER(ctypes.c_int32)],
         "bfgQuadtreeBuild": [_VP, _VP, _VP, _I64, _I64, ctypes.c_int32, _VP, _VP, _I64, _VP],
         "bfgRngSeed": [ctypes.POINTER(_RngC), ctypes.c_uint64],
         "bfgRngUniform1": [ctypes.POINTER(_RngC)],
@@ -380,13 +381,22 @@ class Fac:
         self.close()
 
     def autotune(self, precision: str = "bf16x3", rhs: int = 16):
-        """bfgFacAutotune: per-stage schedules of the tensor-core apply picked
-        by timing; returns (default ms, tuned ms) per stage."""
+        """bfgFacAutotune: the tensor-core apply's RHS tile width and
+        per-stage schedules for `rhs` right-hand sides, picked by timing;
+        returns (default ms, tuned ms) per stage."""
         out = np.zeros(64, dtype=np.float64)
         ns = ctypes.c_int32()
         self.ctx.check(lib().bfgFacAutotune(self.handle, PRECISIONS[precision], int(rhs),
                                             _ptr(out), len(out), ctypes.byref(ns)), "autotune")
         return out[:2 * ns.value].reshape(-1, 2)
+
+    def rhs_tile(self, precision: str = "bf16x3", rhs: int = 16) -> int:
+        """bfgFacGetRhsTile: the RHS tile width (16 or 32) the tensor-core
+        apply of `rhs` right-hand sides uses."""
+        t = ctypes.c_int32()
+        self.ctx.check(lib().bfgFacGetRhsTile(self.handle, PRECISIONS[precision], int(rhs),
+                                              ctypes.byref(t)), "rhs tile")
+        return int(t.value)
 
     def prepare(self, precision: str):
         """Builds the precision's copy of the factors now (bfgFacPrepare)."""

@@ -138,12 +138,15 @@ struct bfgFac_s {
     size_t stages = 0;
     DevBuf arena;
     bfg::ApplyProgram p128;           // the 128-row program the chunks cut
-    // chunk dealings by number of chunk streams: R right-hand sides take
-    // ctas / ceil(R / 16) streams (every tile of every stream resident)
+    // chunk dealings by number of chunk streams: R right-hand sides in
+    // tiles of rt take ctas / ceil(R / rt) streams (every tile of every
+    // stream resident)
     struct Sched {
       DevBuf chunks, ctaChunk0;
     };
     std::map<int32_t, Sched> sched;
+    // RHS tile widths the autotuner chose, by R (else bfg::tcRhsTile(R))
+    std::map<int64_t, int32_t> rhsTile;
   } tc[2];
   DevBuf tcStatus;                  // kStatusTcTimeout from the tensor-core kernel
   uint64_t tcWaitLimitNs = bfg::kTcWaitLimitNs;   // lowered only by the test hook
@@ -776,10 +779,16 @@ void checkTcStatus(bfgFac f) {
   }
 }
 
-// chunk streams for R right-hand sides: the resident CTAs shared out over
-// the RHS tiles of every stream
-int32_t tcStreams(bfgFac_s::Tc const &tc, int64_t R) {
-  int64_t const rt = bfg::tcRhsTile(R);
+// the RHS tile of an apply of R right-hand sides: the autotuner's choice
+// for this R, else the default
+int32_t tcTile(bfgFac_s::Tc const &tc, int64_t R) {
+  auto const it = tc.rhsTile.find(R);
+  return it != tc.rhsTile.end() ? it->second : bfg::tcRhsTile(R);
+}
+
+// chunk streams for R right-hand sides in tiles of rt: the resident CTAs
+// shared out over the RHS tiles of every stream
+int32_t tcStreams(bfgFac_s::Tc const &tc, int64_t R, int32_t rt) {
   int64_t const tiles = (R + rt - 1) / rt;
   return (int32_t)std::max<int64_t>(1, tc.ctas / std::max<int64_t>(1, tiles));
 }
@@ -803,7 +812,8 @@ void runApplyTc(bfgFac f, int terms, float2 const *X, int64_t ldx, int64_t R, fl
   cudaStream_t s = f->ctx->stream;
   bfg::ApplyProgram const &p = f->prog;
   bfgFac_s::Tc &tc = f->tc[terms - 2];
-  int32_t const streams = tcStreams(tc, R);
+  int32_t const rt = tcTile(tc, R);
+  int32_t const streams = tcStreams(tc, R, rt);
   bfgFac_s::Tc::Sched &sched = tcSched(f, terms, streams);
   ck(f->ws.ensure((size_t)std::max<int64_t>(1, p.wsRows) * R * sizeof(float2)), "workspace");
   float2 *W = f->ws.as<float2>();
@@ -824,7 +834,7 @@ void runApplyTc(bfgFac f, int terms, float2 const *X, int64_t ldx, int64_t R, fl
     mark();
   }
   for (size_t st = 0; st < tc.stages; ++st) {
-    ck(bfg::launchApplyTc(terms, sched.chunks.as<bfg::TcChunk>(),
+    ck(bfg::launchApplyTc(terms, rt, sched.chunks.as<bfg::TcChunk>(),
                           sched.ctaChunk0.as<int64_t>() + st * (size_t)(streams + 1), streams,
                           tc.arena.as<uint8_t>(), Xt, ldxt, W, R, f->tcStatus.as<int32_t>(), s,
                           f->tcWaitLimitNs),
@@ -1535,14 +1545,25 @@ bfgStatus bfgFacAutotune(bfgFac f, bfgPrecision prec, int64_t R, double *stageMs
     cudaStream_t s = f->ctx->stream;
     bfg::ApplyProgram const &p128 = tc.p128;
     size_t const nStages = tc.stages;
-    int32_t const ctas = tcStreams(tc, R);
     std::vector<bfg::TcCostModel> const models = bfg::tcCandidateModels();   // default first
     size_t const K = models.size();
-    std::vector<bfg::TcSchedule> cands(K);
-    for (size_t k = 0; k < K; ++k) {
-      bfg::makeTcSchedule(p128, terms, ctas, cands[k], models[k]);
-      if (cands[k].arenaBytes != cands[0].arenaBytes)
-        throw BfgError{BFG_ERROR_RUNTIME, "autotune: schedules disagree on the tiles"};
+    // both RHS tile widths, the default first; per width its own stream count
+    int32_t const widths[2] = {bfg::tcRhsTile(R), bfg::tcRhsTile(R) == 16 ? 32 : 16};
+    struct Width {
+      int32_t rt = 0, ctas = 0;
+      std::vector<bfg::TcSchedule> cands;
+      std::vector<std::vector<float>> best;   // [model][stage] ms
+    } wd[2];
+    for (int w = 0; w < 2; ++w) {
+      wd[w].rt = widths[w];
+      wd[w].ctas = tcStreams(tc, R, widths[w]);
+      wd[w].cands.resize(K);
+      for (size_t k = 0; k < K; ++k) {
+        bfg::makeTcSchedule(p128, terms, wd[w].ctas, wd[w].cands[k], models[k]);
+        if (wd[w].cands[k].arenaBytes != wd[0].cands[0].arenaBytes)
+          throw BfgError{BFG_ERROR_RUNTIME, "autotune: schedules disagree on the tiles"};
+      }
+      wd[w].best.assign(K, std::vector<float>(nStages, 1e30f));
     }
     // scratch operands: the times do not depend on the values
     bfg::ApplyProgram const &p = f->prog;
@@ -1552,57 +1573,77 @@ bfgStatus bfgFacAutotune(bfgFac f, bfgPrecision prec, int64_t R, double *stageMs
     ck(f->ws.ensure((size_t)std::max<int64_t>(1, p.wsRows) * R * sizeof(float2)), "workspace");
     Events const ev(nStages + 1, "autotune");
     int const reps = 5;
-    std::vector<std::vector<float>> best(K, std::vector<float>(nStages, 1e30f));
     DevBuf dch, dc0;
-    for (size_t k = 0; k < K; ++k) {
-      upload(dch, cands[k].chunks, s, "autotune");
-      upload(dc0, cands[k].ctaChunk0, s, "autotune");
-      for (int rep = 0; rep < reps + 1; ++rep) {
-        ck(cudaEventRecord(ev[0], s), "autotune");
-        for (size_t st = 0; st < nStages; ++st) {
-          ck(bfg::launchApplyTc(terms, dch.as<bfg::TcChunk>(),
-                                dc0.as<int64_t>() + st * (size_t)(ctas + 1), ctas,
-                                tc.arena.as<uint8_t>(), xs.as<float2>(), R, f->ws.as<float2>(), R,
-                                f->tcStatus.as<int32_t>(), s),
-             "autotune");
-          ck(cudaEventRecord(ev[st + 1], s), "autotune");
-        }
-        ck(cudaStreamSynchronize(s), "autotune");
-        if (rep == 0) continue;   // warm-up
-        for (size_t st = 0; st < nStages; ++st) {
-          float ms = 0;
-          ck(cudaEventElapsedTime(&ms, ev[st], ev[st + 1]), "autotune");
-          best[k][st] = std::min(best[k][st], ms);
+    for (Width &w : wd)
+      for (size_t k = 0; k < K; ++k) {
+        upload(dch, w.cands[k].chunks, s, "autotune");
+        upload(dc0, w.cands[k].ctaChunk0, s, "autotune");
+        for (int rep = 0; rep < reps + 1; ++rep) {
+          ck(cudaEventRecord(ev[0], s), "autotune");
+          for (size_t st = 0; st < nStages; ++st) {
+            ck(bfg::launchApplyTc(terms, w.rt, dch.as<bfg::TcChunk>(),
+                                  dc0.as<int64_t>() + st * (size_t)(w.ctas + 1), w.ctas,
+                                  tc.arena.as<uint8_t>(), xs.as<float2>(), R, f->ws.as<float2>(),
+                                  R, f->tcStatus.as<int32_t>(), s),
+               "autotune");
+            ck(cudaEventRecord(ev[st + 1], s), "autotune");
+          }
+          ck(cudaStreamSynchronize(s), "autotune");
+          if (rep == 0) continue;   // warm-up
+          for (size_t st = 0; st < nStages; ++st) {
+            float ms = 0;
+            ck(cudaEventElapsedTime(&ms, ev[st], ev[st + 1]), "autotune");
+            w.best[k][st] = std::min(w.best[k][st], ms);
+          }
         }
       }
-    }
     checkTcStatus(f);
-    // per stage the fastest candidate, spliced into one schedule
+    // per width and stage the fastest model; the width with the smaller sum
+    // of those (the default on a tie)
+    std::vector<size_t> pick[2];
+    double total[2] = {0, 0};
+    for (int w = 0; w < 2; ++w)
+      for (size_t st = 0; st < nStages; ++st) {
+        size_t kb = 0;
+        for (size_t k = 1; k < K; ++k)
+          if (wd[w].best[k][st] < wd[w].best[kb][st]) kb = k;
+        pick[w].push_back(kb);
+        total[w] += wd[w].best[kb][st];
+      }
+    int const wb = total[1] < total[0] ? 1 : 0;
+    Width const &win = wd[wb];
+    // the chosen width's per-stage schedules, spliced into one
     std::vector<bfg::TcChunk> chunks;
     std::vector<int64_t> c0;
     for (size_t st = 0; st < nStages; ++st) {
-      size_t kb = 0;
-      for (size_t k = 1; k < K; ++k)
-        if (best[k][st] < best[kb][st]) kb = k;
-      bfg::TcSchedule const &c = cands[kb];
-      int64_t const a = c.ctaChunk0[st * (size_t)(ctas + 1)];
-      int64_t const b = c.ctaChunk0[st * (size_t)(ctas + 1) + ctas];
+      bfg::TcSchedule const &c = win.cands[pick[wb][st]];
+      int64_t const a = c.ctaChunk0[st * (size_t)(win.ctas + 1)];
+      int64_t const b = c.ctaChunk0[st * (size_t)(win.ctas + 1) + win.ctas];
       int64_t const base = (int64_t)chunks.size();
-      for (int32_t q = 0; q <= ctas; ++q) c0.push_back(c.ctaChunk0[st * (size_t)(ctas + 1) + q] - a + base);
+      for (int32_t q = 0; q <= win.ctas; ++q)
+        c0.push_back(c.ctaChunk0[st * (size_t)(win.ctas + 1) + q] - a + base);
       chunks.insert(chunks.end(), c.chunks.begin() + a, c.chunks.begin() + b);
-      if (numStages) *numStages = (int32_t)nStages;
       if ((int64_t)(2 * st + 1) < capacity) {
-        stageMs[2 * st] = best[0][st];
-        stageMs[2 * st + 1] = best[kb][st];
+        stageMs[2 * st] = wd[0].best[0][st];
+        stageMs[2 * st + 1] = win.best[pick[wb][st]][st];
       }
     }
     if (numStages) *numStages = (int32_t)nStages;
-    bfgFac_s::Tc::Sched &tuned = tc.sched[ctas];
+    bfgFac_s::Tc::Sched &tuned = tc.sched[win.ctas];
     upload(tuned.chunks, chunks, s, "tensor-core schedule");
     upload(tuned.ctaChunk0, c0, s, "tensor-core schedule");
     ck(cudaStreamSynchronize(s), "tensor-core schedule");
+    tc.rhsTile[R] = win.rt;
     return BFG_OK;
   });
+}
+
+bfgStatus bfgFacGetRhsTile(bfgFac f, bfgPrecision prec, int64_t R, int32_t *rhsTile) {
+  if (!f || R < 1 || !rhsTile) return BFG_ERROR_INVALID_ARGUMENTS;
+  if (!isTcPrecision(prec))
+    return fail(f->ctx, BFG_ERROR_INVALID_ARGUMENTS, "RHS tile: a tensor-core precision only");
+  *rhsTile = tcTile(f->tc[prec == BFG_PRECISION_BF16X3 ? 1 : 0], R);
+  return BFG_OK;
 }
 
 bfgStatus bfgFacPrepare(bfgFac f, bfgPrecision prec) {

@@ -450,6 +450,7 @@ extern "C" {
 
 bfgStatus bfgSystemBuildCoarse(bfgSystem sys, int32_t extraModes, int64_t *dimOut) {
   if (!sys || extraModes < 0) return BFG_ERROR_INVALID_ARGUMENTS;
+  sys->haveCoarse = false;   // a rebuild that fails leaves no half-built space in use
   cudaStream_t s = sys->stream();
   int64_t const n = sys->n, nb = sys->numCurves;
   double const pi2 = 6.283185307179586;

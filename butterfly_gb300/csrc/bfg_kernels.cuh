@@ -155,18 +155,19 @@ cudaError_t launchApplyReduce(int32_t const *rowSeg, int64_t const *segStart,
 cudaError_t tcPrepare(int32_t terms, int32_t *ctasPerSm);
 cudaError_t launchTcFill(int32_t terms, TcFill const *fills, int64_t nFills,
                          double2 const *arena64, uint8_t *tarena, cudaStream_t stream);
-// one stage: `ctas` chunk streams times ceil(R / tcRhsTile(R)) RHS tiles,
-// one persistent CTA each, the tiles of a stream adjacent in the grid;
-// stream c runs chunks [ctaChunk0[c], ctaChunk0[c+1]); status bit 4 = a
-// bounded wait expired.  The tile is 16 RHS for R <= 16, else 32.
+// one stage: `ctas` chunk streams times ceil(R / rt) RHS tiles of rt = 16
+// or 32 right-hand sides, one persistent CTA each, the tiles of a stream
+// adjacent in the grid; stream c runs chunks [ctaChunk0[c], ctaChunk0[c+1]);
+// status bit 4 = a bounded wait expired.
+// the default tile: 16 RHS for R <= 16, else 32
 int32_t tcRhsTile(int64_t R);
 // every mbarrier wait of the kernel gives up after waitLimitNs (then the CTA
 // drains what it has in flight, frees its tensor memory and sets status bit 4)
 constexpr uint64_t kTcWaitLimitNs = 1000000000ull;
-cudaError_t launchApplyTc(int32_t terms, TcChunk const *chunks, int64_t const *ctaChunk0,
-                          int32_t ctas, uint8_t const *tarena, float2 const *X, int64_t ldx,
-                          float2 *W, int64_t R, int32_t *status, cudaStream_t stream,
-                          uint64_t waitLimitNs = kTcWaitLimitNs);
+cudaError_t launchApplyTc(int32_t terms, int32_t rt, TcChunk const *chunks,
+                          int64_t const *ctaChunk0, int32_t ctas, uint8_t const *tarena,
+                          float2 const *X, int64_t ldx, float2 *W, int64_t R, int32_t *status,
+                          cudaStream_t stream, uint64_t waitLimitNs = kTcWaitLimitNs);
 enum : int32_t { kStatusTcTimeout = 4 };
 
 // X_tree[i] = X[perm[i]] (row gather, R columns)

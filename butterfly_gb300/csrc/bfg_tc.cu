@@ -810,12 +810,12 @@ cudaError_t launchTcFill(int32_t terms, TcFill const *fills, int64_t nFills,
   return cudaGetLastError();
 }
 
-cudaError_t launchApplyTc(int32_t terms, TcChunk const *chunks, int64_t const *ctaChunk0,
-                          int32_t ctas, uint8_t const *tarena, float2 const *X, int64_t ldx,
-                          float2 *W, int64_t R, int32_t *status, cudaStream_t stream,
-                          uint64_t waitLimitNs) {
+cudaError_t launchApplyTc(int32_t terms, int32_t rt, TcChunk const *chunks,
+                          int64_t const *ctaChunk0, int32_t ctas, uint8_t const *tarena,
+                          float2 const *X, int64_t ldx, float2 *W, int64_t R, int32_t *status,
+                          cudaStream_t stream, uint64_t waitLimitNs) {
+  if (rt != 16 && rt != 32) return cudaErrorInvalidValue;
   if (ctas == 0) return cudaSuccess;
-  int32_t const rt = tcRhsTile(R);
   int64_t const tiles = (R + rt - 1) / rt;
   if (tiles > 0x7fffffff / ctas) return cudaErrorInvalidValue;
   dim3 grid((unsigned)(ctas * tiles));

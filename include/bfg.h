@@ -228,15 +228,28 @@ bfgStatus bfgFacPrepare(bfgFac fac, bfgPrecision precision);
  * how the tests drive that path. */
 bfgStatus bfgFacSetTcWaitLimit(bfgFac fac, uint64_t waitLimitNs);
 
-/* Autotuner of the tensor-core apply (BF16X2, BF16X3): deals each stage's
- * chunks to the persistent CTAs under several cost models, times every
- * stage of every candidate on the GPU (numRhs right-hand sides, best of 5)
- * and keeps, per stage, the fastest (the default model is a candidate, so
- * no stage gets slower).  stageMs[2 s], stageMs[2 s + 1]: stage s with the
- * default and the chosen schedule (up to `capacity` values); *numStages the
- * number of stages.  Results do not change, only which CTA runs which chunk. */
+/* Autotuner of the tensor-core apply (BF16X2, BF16X3) for numRhs
+ * right-hand sides.  It tries both RHS tile widths (16 and 32 right-hand
+ * sides per CTA) and, for each, deals every stage's chunks to the
+ * persistent CTAs under several cost models; it times every stage of every
+ * candidate on the GPU (best of 5).  Per width it takes each stage's
+ * fastest dealing, and it keeps the width whose stages sum to less (the
+ * default width and model are candidates, so the apply gets no slower).
+ * Later applies of numRhs right-hand sides use the choice.
+ * stageMs[2 s], stageMs[2 s + 1]: stage s with the default width and
+ * schedule, and with the chosen ones (up to `capacity` values);
+ * *numStages the number of stages.  Within one tile width the results do
+ * not change, only which CTA runs which chunk; the two widths sum the
+ * plane products in different groupings, so a change of width changes
+ * results by rounding. */
 bfgStatus bfgFacAutotune(bfgFac fac, bfgPrecision precision, int64_t numRhs, double *stageMs,
                          int32_t capacity, int32_t *numStages);
+
+/* The RHS tile width (16 or 32) the tensor-core apply of numRhs right-hand
+ * sides uses in this precision: bfgFacAutotune's choice for that count,
+ * else the default (16 up to 16 right-hand sides, else 32). */
+bfgStatus bfgFacGetRhsTile(bfgFac fac, bfgPrecision precision, int64_t numRhs,
+                           int32_t *rhsTile);
 
 /* Waits for the context's stream and reports what the tensor-core applies
  * enqueued since the last check left in their status word:

@@ -171,21 +171,35 @@ def test_pipelined_host_apply_matches_synchronous(ctx, prec):
         assert np.array_equal(y.numpy(), fac.apply(x, precision=prec))
 
 
-@pytest.mark.parametrize("R", [16, 64])
-def test_autotune_keeps_results_and_never_slows_a_stage(ctx, R):
-    """bfgFacAutotune re-deals chunks to CTAs; an item stays on one CTA with
-    its chunks in order, so the results are bit-identical (16- and 32-RHS
-    tiles)."""
+@pytest.mark.parametrize("R", [16, 24, 64])
+def test_autotune_keeps_results_and_never_slows_the_apply(ctx, R):
+    """bfgFacAutotune picks the RHS tile width and re-deals chunks to CTAs.
+    An item stays on one CTA with its chunks in order, so within a width the
+    results are bit-identical; a change of width regroups the plane
+    products' sums, within rounding.  The default is a candidate, so the
+    tuned stages sum to no more than the default ones."""
     g, fac = golden_fac("ellipse_n16384_k128", ctx)
     X = torch.from_numpy(O.RefRng(50).complex_randn(16384 * R).reshape(16384, R)).cuda()
     X = X.to(torch.complex64)
+    assert fac.rhs_tile("bf16x3", R) == (16 if R <= 16 else 32)
     y0 = fac.apply(X, precision="bf16x3")
     times = fac.autotune("bf16x3", R)
     assert times.shape[0] == len(fac.launch_info()) - 1          # stages, not the final sum
-    assert np.all(times[:, 1] <= times[:, 0])
-    assert torch.equal(fac.apply(X, precision="bf16x3"), y0)
+    assert times[:, 1].sum() <= times[:, 0].sum()
+    rt = fac.rhs_tile("bf16x3", R)
+    assert rt in (16, 32)
+    y1 = fac.apply(X, precision="bf16x3")
+    if rt == (16 if R <= 16 else 32):
+        assert torch.equal(y1, y0)
+    else:
+        assert rel_err(y1.cpu().numpy().astype(np.complex128),
+                       y0.cpu().numpy().astype(np.complex128)) < TOL["bf16x3"] / 3
+    # the choice holds for this R only
+    assert fac.rhs_tile("bf16x3", R + 1) == (16 if R + 1 <= 16 else 32)
     with pytest.raises(B.BfgError):
         fac.autotune("fp32", 16)
+    with pytest.raises(B.BfgError):
+        fac.rhs_tile("fp32", 16)
 
 
 def test_double_float_jacobi_factorization(ctx):
