@@ -807,37 +807,59 @@ bfgFac_s::Tc::Sched &tcSched(bfgFac f, int terms, int32_t streams) {
   return d;
 }
 
+// xTiled > 0: X is already tile-major (tcInputTiling's layout: panel t of
+// rt columns at X + t xTiled, leading dimension rt), as the host-operand
+// applies convert it, so the first stage's full tiles arrive by bulk copies
+// too; tree order only
 void runApplyTc(bfgFac f, int terms, float2 const *X, int64_t ldx, int64_t R, float2 *Y,
-                int64_t ldy, uint32_t flags, std::vector<cudaEvent_t> *events) {
+                int64_t ldy, uint32_t flags, std::vector<cudaEvent_t> *events,
+                int64_t xTiled = 0) {
   cudaStream_t s = f->ctx->stream;
   bfg::ApplyProgram const &p = f->prog;
   bfgFac_s::Tc &tc = f->tc[terms - 2];
   int32_t const rt = tcTile(tc, R);
   int32_t const streams = tcStreams(tc, R, rt);
   bfgFac_s::Tc::Sched &sched = tcSched(f, terms, streams);
-  ck(f->ws.ensure((size_t)std::max<int64_t>(1, p.wsRows) * R * sizeof(float2)), "workspace");
+  // With more than one RHS tile the workspace is tile-major (one panel of rt
+  // columns per tile), so that every stage after the first brings a full
+  // tile's input rows by one bulk copy; so is the gathered input of an
+  // original-order apply.  One tile is row-major.
+  int64_t const tiles = (R + rt - 1) / rt;
+  bool const tiled = tiles > 1;
+  int64_t const wsRows = std::max<int64_t>(1, p.wsRows);
+  int64_t const ldw = tiled ? rt : R, wTs = tiled ? wsRows * rt : rt;
+  ck(f->ws.ensure((size_t)wsRows * (tiled ? tiles * rt : R) * sizeof(float2)), "workspace");
   float2 *W = f->ws.as<float2>();
   float2 const *Xt = X;
-  int64_t ldxt = ldx;
+  int64_t ldxt = ldx, xTs = rt;
+  if (xTiled) {
+    if (!tiled || (flags & BFG_APPLY_ORIGINAL_ORDER) || xTiled < p.numCols * rt)
+      throw BfgError{BFG_ERROR_RUNTIME, "tensor-core apply: bad tile-major input"};
+    ldxt = rt;
+    xTs = xTiled;
+  }
   size_t ev = 0;
   auto mark = [&]() {
     if (events) ck(cudaEventRecord((*events)[ev++], s), "event");
   };
   mark();
   if (flags & BFG_APPLY_ORIGINAL_ORDER) {
-    ck(f->xbuf.ensure((size_t)p.numCols * R * sizeof(float2)), "gather buffer");
+    ck(f->xbuf.ensure((size_t)p.numCols * (tiled ? tiles * rt : R) * sizeof(float2)),
+       "gather buffer");
     ck(bfg::launchGatherRows<float2>(X, ldx, f->srcPerm.as<int64_t>(), p.numCols, R,
-                                     f->xbuf.as<float2>(), s),
+                                     f->xbuf.as<float2>(), s, tiled ? rt : 0,
+                                     tiled ? p.numCols * rt : 0),
        "gather");
     Xt = f->xbuf.as<float2>();
-    ldxt = R;
+    ldxt = tiled ? rt : R;
+    xTs = tiled ? p.numCols * rt : rt;
     mark();
   }
   for (size_t st = 0; st < tc.stages; ++st) {
     ck(bfg::launchApplyTc(terms, rt, sched.chunks.as<bfg::TcChunk>(),
                           sched.ctaChunk0.as<int64_t>() + st * (size_t)(streams + 1), streams,
-                          tc.arena.as<uint8_t>(), Xt, ldxt, W, R, f->tcStatus.as<int32_t>(), s,
-                          f->tcWaitLimitNs),
+                          tc.arena.as<uint8_t>(), Xt, ldxt, xTs, W, ldw, wTs, R,
+                          f->tcStatus.as<int32_t>(), s, f->tcWaitLimitNs),
        "tensor-core apply stage");
     mark();
   }
@@ -846,7 +868,7 @@ void runApplyTc(bfgFac f, int terms, float2 const *X, int64_t ldx, int64_t R, fl
                                     Y, ldy, p.numRows,
                                     (flags & BFG_APPLY_ORIGINAL_ORDER) ? f->tgtPerm.as<int64_t>()
                                                                       : nullptr,
-                                    s),
+                                    s, tiled ? rt : 0, tiled ? wTs : 0),
      "apply reduce");
   mark();
 }
@@ -884,6 +906,28 @@ bfgStatus applyDispatch(bfgFac f, bfgPrecision prec, void const *X, int64_t ldx,
   } else {
     return fail(f->ctx, BFG_ERROR_NOT_IMPLEMENTED, "apply: unknown precision");
   }
+  return BFG_OK;
+}
+
+// The host-operand applies convert their complex128 input to complex64 for
+// the FP32 and tensor-core precisions.  A tensor-core apply of more than one
+// RHS tile in tree order takes that input tile-major (panel t of rt columns
+// at t x numCols x rt, leading dimension rt), so the conversion writes that
+// layout and the first stage bulk-copies full tiles too.  Returns the panel
+// stride, 0 for a row-major input; *rt the tile.
+int64_t tcInputTiling(bfgFac f, bfgPrecision prec, int64_t R, uint32_t flags, int32_t *rt) {
+  *rt = 0;
+  if (!isTcPrecision(prec) || (flags & BFG_APPLY_ORIGINAL_ORDER)) return 0;
+  *rt = tcTile(f->tc[prec == BFG_PRECISION_BF16X3 ? 1 : 0], R);
+  return R > *rt ? f->prog.numCols * *rt : 0;
+}
+
+// the tensor-core apply of a tile-major input (tcInputTiling)
+bfgStatus applyTcTiledInput(bfgFac f, bfgPrecision prec, float2 const *X, int64_t xTiled,
+                            int64_t R, float2 *Y, int64_t ldy, uint32_t flags) {
+  int const terms = prec == BFG_PRECISION_BF16X3 ? 3 : 2;
+  ensureTc(f, terms);
+  runApplyTc(f, terms, X, tcTile(f->tc[terms - 2], R), R, Y, ldy, flags, nullptr, xTiled);
   return BFG_OK;
 }
 
@@ -1503,11 +1547,17 @@ bfgStatus bfgFacApplyHost(bfgFac f, bfgPrecision prec, double const *X, int64_t 
       bfgStatus st = applyDispatch(f, prec, f->hx128.p, R, R, f->hy128.p, R, flags, nullptr);
       if (st != BFG_OK) return st;
     } else if (prec == BFG_PRECISION_FP32 || isTcPrecision(prec)) {
-      ck(f->hx64.ensure((size_t)nc * R * 8), "apply buffers");
+      int32_t rt = 0;
+      int64_t const xTiled = tcInputTiling(f, prec, R, flags, &rt);
+      ck(f->hx64.ensure((size_t)nc * (xTiled ? (R + rt - 1) / rt * rt : R) * 8), "apply buffers");
       ck(f->hy64.ensure((size_t)nr * R * 8), "apply buffers");
-      ck(bfg::launchC128ToC64(f->hx128.as<double2>(), R, nc, R, f->hx64.as<float2>(), R, s),
+      ck(bfg::launchC128ToC64(f->hx128.as<double2>(), R, nc, R, f->hx64.as<float2>(), R, s,
+                              xTiled ? rt : 0, xTiled),
          "convert X");
-      bfgStatus st = applyDispatch(f, prec, f->hx64.p, R, R, f->hy64.p, R, flags, nullptr);
+      bfgStatus st =
+          xTiled ? applyTcTiledInput(f, prec, f->hx64.as<float2>(), xTiled, R, f->hy64.as<float2>(),
+                                     R, flags)
+                 : applyDispatch(f, prec, f->hx64.p, R, R, f->hy64.p, R, flags, nullptr);
       if (st != BFG_OK) return st;
       ck(bfg::launchC64ToC128(f->hy64.as<float2>(), R, nr, R, f->hy128.as<double2>(), R, s),
          "convert Y");
@@ -1565,12 +1615,15 @@ bfgStatus bfgFacAutotune(bfgFac f, bfgPrecision prec, int64_t R, double *stageMs
       }
       wd[w].best.assign(K, std::vector<float>(nStages, 1e30f));
     }
-    // scratch operands: the times do not depend on the values
+    // scratch operands: the times do not depend on the values; the input
+    // row-major, the workspace laid out as the apply lays it out (tile-major
+    // with more than one tile)
     bfg::ApplyProgram const &p = f->prog;
+    int64_t const wsRows = std::max<int64_t>(1, p.wsRows);
     DevBuf xs;
     ck(xs.ensure((size_t)std::max<int64_t>(1, p.numCols) * R * sizeof(float2)), "autotune");
     ck(cudaMemsetAsync(xs.p, 0, (size_t)p.numCols * R * sizeof(float2), s), "autotune");
-    ck(f->ws.ensure((size_t)std::max<int64_t>(1, p.wsRows) * R * sizeof(float2)), "workspace");
+    ck(f->ws.ensure((size_t)wsRows * ((R + 31) / 32) * 32 * sizeof(float2)), "workspace");
     Events const ev(nStages + 1, "autotune");
     int const reps = 5;
     DevBuf dch, dc0;
@@ -1581,10 +1634,12 @@ bfgStatus bfgFacAutotune(bfgFac f, bfgPrecision prec, int64_t R, double *stageMs
         for (int rep = 0; rep < reps + 1; ++rep) {
           ck(cudaEventRecord(ev[0], s), "autotune");
           for (size_t st = 0; st < nStages; ++st) {
+            bool const tiled = R > w.rt;
             ck(bfg::launchApplyTc(terms, w.rt, dch.as<bfg::TcChunk>(),
                                   dc0.as<int64_t>() + st * (size_t)(w.ctas + 1), w.ctas,
-                                  tc.arena.as<uint8_t>(), xs.as<float2>(), R, f->ws.as<float2>(),
-                                  R, f->tcStatus.as<int32_t>(), s),
+                                  tc.arena.as<uint8_t>(), xs.as<float2>(), R, w.rt,
+                                  f->ws.as<float2>(), tiled ? w.rt : R,
+                                  tiled ? wsRows * w.rt : w.rt, R, f->tcStatus.as<int32_t>(), s),
                "autotune");
             ck(cudaEventRecord(ev[st + 1], s), "autotune");
           }
@@ -1677,10 +1732,12 @@ bfgStatus bfgFacApplyHostAsync(bfgFac f, bfgPrecision prec, double const *X, int
     cudaStream_t const cs = f->ctx->stream, up = f->upStream, down = f->downStream;
     int64_t const nr = f->prog.numRows, nc = f->prog.numCols;
     auto &h = f->hslot[f->asyncCalls & 1];
+    int32_t rt = 0;
+    int64_t const xTiled = tcInputTiling(f, prec, R, flags, &rt);
     ck(h.x128.ensure((size_t)nc * R * 16), "apply buffers");
     ck(h.y128.ensure((size_t)nr * R * 16), "apply buffers");
     if (!c128) {
-      ck(h.x64.ensure((size_t)nc * R * 8), "apply buffers");
+      ck(h.x64.ensure((size_t)nc * (xTiled ? (R + rt - 1) / rt * rt : R) * 8), "apply buffers");
       ck(h.y64.ensure((size_t)nr * R * 8), "apply buffers");
     }
     // upload, once the compute of this slot's previous call has read it
@@ -1700,10 +1757,14 @@ bfgStatus bfgFacApplyHostAsync(bfgFac f, bfgPrecision prec, double const *X, int
       if (st != BFG_OK) return st;
       ck(cudaEventRecord(h.consumed, cs), "order");
     } else {
-      ck(bfg::launchC128ToC64(h.x128.as<double2>(), R, nc, R, h.x64.as<float2>(), R, cs),
+      ck(bfg::launchC128ToC64(h.x128.as<double2>(), R, nc, R, h.x64.as<float2>(), R, cs,
+                              xTiled ? rt : 0, xTiled),
          "convert X");
       ck(cudaEventRecord(h.consumed, cs), "order");
-      bfgStatus st = applyDispatch(f, prec, h.x64.p, R, R, h.y64.p, R, flags, nullptr);
+      bfgStatus st =
+          xTiled ? applyTcTiledInput(f, prec, h.x64.as<float2>(), xTiled, R, h.y64.as<float2>(), R,
+                                     flags)
+                 : applyDispatch(f, prec, h.x64.p, R, R, h.y64.p, R, flags, nullptr);
       if (st != BFG_OK) return st;
       ck(bfg::launchC64ToC128(h.y64.as<float2>(), R, nr, R, h.y128.as<double2>(), R, cs),
          "convert Y");

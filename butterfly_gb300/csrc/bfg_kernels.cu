@@ -681,13 +681,14 @@ __global__ void arenaToF32Kernel(double2 const *a, float2 *b, int64_t n) {
 }
 
 __global__ void c128ToC64Kernel(double2 const *a, int64_t lda, int64_t rows, int64_t cols,
-                                float2 *b, int64_t ldb) {
+                                float2 *b, int64_t ldb, int64_t bTile, int64_t bTileStride) {
   int64_t const total = rows * cols;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
     int64_t const i = e / cols, j = e % cols;
     double2 v = a[i * lda + j];
-    b[i * ldb + j] = make_float2((float)v.x, (float)v.y);
+    int64_t const o = bTile ? (j / bTile) * bTileStride + i * bTile + j % bTile : i * ldb + j;
+    b[o] = make_float2((float)v.x, (float)v.y);
   }
 }
 
@@ -1000,7 +1001,8 @@ __global__ void applyReduceKernel(int32_t const *__restrict__ rowSeg,
                                   int64_t const *__restrict__ segBase,
                                   T2 const *__restrict__ W, int64_t R,
                                   T2 *__restrict__ Y, int64_t ldy, int64_t nRows,
-                                  int64_t const *__restrict__ outPerm) {
+                                  int64_t const *__restrict__ outPerm, int64_t wTile,
+                                  int64_t wTileStride) {
   using T = typename Real<T2>::T;
   int64_t const total = nRows * R;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
@@ -1008,9 +1010,12 @@ __global__ void applyReduceKernel(int32_t const *__restrict__ rowSeg,
     int64_t const i = e / R, r = e % R;
     int const s = rowSeg[i];
     int64_t const di = i - segStart[s];
+    // W row-major (ld R), or tile-major: panels of wTile columns
+    T2 const *Wc = wTile ? W + (r / wTile) * wTileStride + r % wTile : W + r;
+    int64_t const ldw = wTile ? wTile : R;
     T sr = 0, si = 0;
     for (int64_t c = segContrib0[s]; c < segContrib0[s + 1]; ++c) {
-      T2 const v = W[(segBase[c] + di) * R + r];
+      T2 const v = Wc[(segBase[c] + di) * ldw];
       sr += v.x;
       si += v.y;
     }
@@ -1021,12 +1026,14 @@ __global__ void applyReduceKernel(int32_t const *__restrict__ rowSeg,
 
 template <typename T2>
 __global__ void gatherRowsKernel(T2 const *X, int64_t ldx, int64_t const *perm,
-                                 int64_t nRows, int64_t R, T2 *out) {
+                                 int64_t nRows, int64_t R, T2 *out, int64_t outTile,
+                                 int64_t outTileStride) {
   int64_t const total = nRows * R;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
     int64_t const i = e / R, r = e % R;
-    out[e] = X[perm[i] * ldx + r];
+    int64_t const o = outTile ? (r / outTile) * outTileStride + i * outTile + r % outTile : e;
+    out[o] = X[perm[i] * ldx + r];
   }
 }
 
@@ -1176,9 +1183,11 @@ cudaError_t launchArenaToF32(double2 const *a64, float2 *a32, int64_t n, cudaStr
 }
 
 cudaError_t launchC128ToC64(double2 const *a, int64_t lda, int64_t rows, int64_t cols,
-                            float2 *b, int64_t ldb, cudaStream_t stream) {
+                            float2 *b, int64_t ldb, cudaStream_t stream, int64_t bTile,
+                            int64_t bTileStride) {
   if (rows * cols == 0) return cudaSuccess;
-  c128ToC64Kernel<<<gridFor(rows * cols, 256), 256, 0, stream>>>(a, lda, rows, cols, b, ldb);
+  c128ToC64Kernel<<<gridFor(rows * cols, 256), 256, 0, stream>>>(a, lda, rows, cols, b, ldb,
+                                                                 bTile, bTileStride);
   return cudaGetLastError();
 }
 
@@ -1234,17 +1243,18 @@ cudaError_t launchApplyReduce(int32_t const *rowSeg, int64_t const *segStart,
                               int64_t const *segContrib0, int64_t const *segBase,
                               T2 const *W, int64_t R, T2 *Y, int64_t ldy,
                               int64_t nRows, int64_t const *outPerm,
-                              cudaStream_t stream) {
+                              cudaStream_t stream, int64_t wTile, int64_t wTileStride) {
   applyReduceKernel<T2><<<gridFor(nRows * R, 256), 256, 0, stream>>>(
-      rowSeg, segStart, segContrib0, segBase, W, R, Y, ldy, nRows, outPerm);
+      rowSeg, segStart, segContrib0, segBase, W, R, Y, ldy, nRows, outPerm, wTile, wTileStride);
   return cudaGetLastError();
 }
 
 template <typename T2>
 cudaError_t launchGatherRows(T2 const *X, int64_t ldx, int64_t const *perm,
-                             int64_t nRows, int64_t R, T2 *out, cudaStream_t stream) {
+                             int64_t nRows, int64_t R, T2 *out, cudaStream_t stream,
+                             int64_t outTile, int64_t outTileStride) {
   gatherRowsKernel<T2><<<gridFor(nRows * R, 256), 256, 0, stream>>>(X, ldx, perm, nRows, R,
-                                                                    out);
+                                                                    out, outTile, outTileStride);
   return cudaGetLastError();
 }
 
@@ -1257,13 +1267,14 @@ template cudaError_t launchApplyStage<float2>(ApplyItem const *, int64_t, ApplyC
 template cudaError_t launchApplyReduce<double2>(int32_t const *, int64_t const *, int64_t const *,
                                                 int64_t const *, double2 const *, int64_t,
                                                 double2 *, int64_t, int64_t, int64_t const *,
-                                                cudaStream_t);
+                                                cudaStream_t, int64_t, int64_t);
 template cudaError_t launchApplyReduce<float2>(int32_t const *, int64_t const *, int64_t const *,
                                                int64_t const *, float2 const *, int64_t, float2 *,
-                                               int64_t, int64_t, int64_t const *, cudaStream_t);
+                                               int64_t, int64_t, int64_t const *, cudaStream_t,
+                                               int64_t, int64_t);
 template cudaError_t launchGatherRows<double2>(double2 const *, int64_t, int64_t const *, int64_t,
-                                               int64_t, double2 *, cudaStream_t);
+                                               int64_t, double2 *, cudaStream_t, int64_t, int64_t);
 template cudaError_t launchGatherRows<float2>(float2 const *, int64_t, int64_t const *, int64_t,
-                                              int64_t, float2 *, cudaStream_t);
+                                              int64_t, float2 *, cudaStream_t, int64_t, int64_t);
 
 }  // namespace bfg

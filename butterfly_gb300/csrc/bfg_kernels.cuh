@@ -131,8 +131,11 @@ cudaError_t launchApplyReduceDf(int32_t const *rowSeg, int64_t const *segStart,
                                 int64_t nRows, int64_t const *outPerm, cudaStream_t stream);
 
 // complex128 <-> complex64 matrix conversion (row-major, leading dims)
+// (bTile > 0: b tile-major, panel t of bTile columns at b + t bTileStride,
+// leading dimension bTile)
 cudaError_t launchC128ToC64(double2 const *a, int64_t lda, int64_t rows, int64_t cols,
-                            float2 *b, int64_t ldb, cudaStream_t stream);
+                            float2 *b, int64_t ldb, cudaStream_t stream, int64_t bTile = 0,
+                            int64_t bTileStride = 0);
 cudaError_t launchC64ToC128(float2 const *a, int64_t lda, int64_t rows, int64_t cols,
                             double2 *b, int64_t ldb, cudaStream_t stream);
 
@@ -143,12 +146,14 @@ cudaError_t launchApplyStage(ApplyItem const *items, int64_t nItems,
                              T2 const *X, int64_t ldx, T2 *W, int64_t R,
                              cudaStream_t stream);
 
+// W row-major with leading dimension R, or (wTile > 0) tile-major: panel t
+// of wTile columns at W + t wTileStride, leading dimension wTile
 template <typename T2>
 cudaError_t launchApplyReduce(int32_t const *rowSeg, int64_t const *segStart,
                               int64_t const *segContrib0, int64_t const *segBase,
                               T2 const *W, int64_t R, T2 *Y, int64_t ldy,
                               int64_t nRows, int64_t const *outPerm,
-                              cudaStream_t stream);
+                              cudaStream_t stream, int64_t wTile = 0, int64_t wTileStride = 0);
 
 // Split-BF16 tensor-core apply (terms = 2 or 3 bf16 planes).
 // sets the kernels' shared-memory limit; returns resident CTAs per SM
@@ -164,15 +169,23 @@ int32_t tcRhsTile(int64_t R);
 // every mbarrier wait of the kernel gives up after waitLimitNs (then the CTA
 // drains what it has in flight, frees its tensor memory and sets status bit 4)
 constexpr uint64_t kTcWaitLimitNs = 1000000000ull;
+// X (inputs) and W (intermediates and outputs) are each row-major (ld >= R,
+// tile stride rt) or, with more than one tile, tile-major: one panel of rt
+// columns per tile (ld = rt, tile stride >= rows x rt), which lets every
+// full tile's rows arrive by one bulk copy per chunk.
 cudaError_t launchApplyTc(int32_t terms, int32_t rt, TcChunk const *chunks,
                           int64_t const *ctaChunk0, int32_t ctas, uint8_t const *tarena,
-                          float2 const *X, int64_t ldx, float2 *W, int64_t R, int32_t *status,
-                          cudaStream_t stream, uint64_t waitLimitNs = kTcWaitLimitNs);
+                          float2 const *X, int64_t ldx, int64_t xTs, float2 *W, int64_t ldw,
+                          int64_t wTs, int64_t R, int32_t *status, cudaStream_t stream,
+                          uint64_t waitLimitNs = kTcWaitLimitNs);
 enum : int32_t { kStatusTcTimeout = 4 };
 
-// X_tree[i] = X[perm[i]] (row gather, R columns)
+// X_tree[i] = X[perm[i]] (row gather, R columns) into out row-major
+// (leading dimension R) or (outTile > 0) tile-major: panel t of outTile
+// columns at out + t outTileStride, leading dimension outTile
 template <typename T2>
 cudaError_t launchGatherRows(T2 const *X, int64_t ldx, int64_t const *perm,
-                             int64_t nRows, int64_t R, T2 *out, cudaStream_t stream);
+                             int64_t nRows, int64_t R, T2 *out, cudaStream_t stream,
+                             int64_t outTile = 0, int64_t outTileStride = 0);
 
 }  // namespace bfg

@@ -345,9 +345,9 @@ __global__ void __launch_bounds__(256) tcFillKernel(TcFill const *__restrict__ f
 template <int TERMS, int RT>
 __global__ void __launch_bounds__(TcLayout<TERMS, RT>::kThreads, 1) applyTcKernel(
     TcChunk const *__restrict__ chunks, int64_t const *__restrict__ ctaChunk0,
-    uint8_t const *__restrict__ tarena, float2 const *__restrict__ X, int64_t ldx,
-    float2 *__restrict__ W, int64_t R, int32_t rhsTiles, int32_t xBulk, uint64_t waitLimitNs,
-    int32_t *status) {
+    uint8_t const *__restrict__ tarena, float2 const *__restrict__ X, int64_t ldx, int64_t xTs,
+    float2 *__restrict__ W, int64_t ldw, int64_t wTs, int64_t R, int32_t rhsTiles, int32_t xBulk,
+    uint64_t waitLimitNs, int32_t *status) {
   using L = TcLayout<TERMS, RT>;
   constexpr int kN = L::kN;
   constexpr int kBuilders = L::kBuilders, kExtractors = L::kExtractors;
@@ -367,11 +367,16 @@ __global__ void __launch_bounds__(TcLayout<TERMS, RT>::kThreads, 1) applyTcKerne
   if (nCh <= 0) return;
   int64_t const r0 = (int64_t)tile * RT;
   int const nr = (R - r0) < RT ? (int)(R - r0) : RT;
+  // this tile's right-hand sides: row i at Xt + i ldx (inputs), Wt + i ldw
+  // (intermediates and outputs); the tile stride is RT for row-major
+  // operands and rows x RT for tile-major ones
+  float2 const *__restrict__ Xt = X + tile * xTs;
+  float2 *__restrict__ Wt = W + tile * wTs;
   TcChunk const *ch = chunks + c0;
   // a chunk's right-hand sides arrive by one bulk copy with its A planes when
-  // they form a contiguous 16-byte aligned block (RT RHS, leading dimension
-  // RT), else by the builders' cp.async (one copy per 128 B row was slower:
-  // the copy engine takes small copies one at a time)
+  // they form a contiguous 16-byte aligned block (a full tile of RT RHS,
+  // leading dimension RT), else by the builders' cp.async (one copy per
+  // 128 B row was slower: the copy engine takes small copies one at a time)
   bool const bulkX = nr == RT && (xBulk & kTcBulkX);
   bool const bulkW = nr == RT && (xBulk & kTcBulkW);
 
@@ -440,7 +445,7 @@ __global__ void __launch_bounds__(TcLayout<TERMS, RT>::kThreads, 1) applyTcKerne
         // the chunk's input rows are one contiguous block (leading dimension RT)
         if (bulk)
           bulkG2S(sbase + s * L::stageBytes + L::aBytes + L::bBytes,
-                  (inIsX ? X : W) + inRow * RT, (uint32_t)nc * (RT * 8), fullX + 8 * s);
+                  (inIsX ? Xt : Wt) + inRow * RT, (uint32_t)nc * (RT * 8), fullX + 8 * s);
         mbarExpectTx(fullA + 8 * s, plane * TERMS);
 #pragma unroll
         for (int t = 0; t < TERMS; ++t)
@@ -566,8 +571,8 @@ __global__ void __launch_bounds__(TcLayout<TERMS, RT>::kThreads, 1) applyTcKerne
       static_assert(kPasses * kJgPass == kTcChunkCols / 4, "builder passes");
       int const q = tid % RT, jgBase = tid / RT;
       auto issueX = [&](Cd const &d, int64_t i) {
-        int64_t const xld = d.inIsX ? ldx : R;
-        float2 const *src = (d.inIsX ? X : W) + d.inRow * xld + r0 + q;
+        int64_t const xld = d.inIsX ? ldx : ldw;
+        float2 const *src = (d.inIsX ? Xt : Wt) + d.inRow * xld + q;
         uint32_t const xs = sbase + (int)(i % S) * L::stageBytes + L::aBytes + L::bBytes;
         if (q < nr)
 #pragma unroll
@@ -724,7 +729,7 @@ __global__ void __launch_bounds__(TcLayout<TERMS, RT>::kThreads, 1) applyTcKerne
           // M = 64 chunks (items of <= 64 rows): lanes 16..31 hold no row
           int const row = d.rows <= 64 ? (lane < 16 ? e * 16 + lane : kTcRows) : e * 32 + lane;
           if (row < d.rows) {
-            float2 *out = W + (d.outRow + row) * R + r0 + 16 * h;
+            float2 *out = Wt + (d.outRow + row) * ldw + 16 * h;
 #pragma unroll
             for (int c = 0; c < 16; ++c)
               if (16 * h + c < nr) out[c] = make_float2(acc[c], acc[16 + c]);
@@ -780,11 +785,12 @@ cudaError_t prepareOne(int *per) {
 }
 template <int TERMS, int RT>
 void launchOne(dim3 grid, cudaStream_t stream, TcChunk const *chunks, int64_t const *ctaChunk0,
-               uint8_t const *tarena, float2 const *X, int64_t ldx, float2 *W, int64_t R,
-               int32_t tiles, int32_t xBulk, uint64_t waitLimitNs, int32_t *status) {
+               uint8_t const *tarena, float2 const *X, int64_t ldx, int64_t xTs, float2 *W,
+               int64_t ldw, int64_t wTs, int64_t R, int32_t tiles, int32_t xBulk,
+               uint64_t waitLimitNs, int32_t *status) {
   applyTcKernel<TERMS, RT><<<grid, TcLayout<TERMS, RT>::kThreads, TcLayout<TERMS, RT>::smemBytes,
                              stream>>>(
-      chunks, ctaChunk0, tarena, X, ldx, W, R, tiles, xBulk, waitLimitNs, status);
+      chunks, ctaChunk0, tarena, X, ldx, xTs, W, ldw, wTs, R, tiles, xBulk, waitLimitNs, status);
 }
 }  // namespace
 
@@ -812,28 +818,38 @@ cudaError_t launchTcFill(int32_t terms, TcFill const *fills, int64_t nFills,
 
 cudaError_t launchApplyTc(int32_t terms, int32_t rt, TcChunk const *chunks,
                           int64_t const *ctaChunk0, int32_t ctas, uint8_t const *tarena,
-                          float2 const *X, int64_t ldx, float2 *W, int64_t R, int32_t *status,
-                          cudaStream_t stream, uint64_t waitLimitNs) {
+                          float2 const *X, int64_t ldx, int64_t xTs, float2 *W, int64_t ldw,
+                          int64_t wTs, int64_t R, int32_t *status, cudaStream_t stream,
+                          uint64_t waitLimitNs) {
   if (rt != 16 && rt != 32) return cudaErrorInvalidValue;
   if (ctas == 0) return cudaSuccess;
   int64_t const tiles = (R + rt - 1) / rt;
   if (tiles > 0x7fffffff / ctas) return cudaErrorInvalidValue;
+  // row-major operands hold a tile's RT columns side by side (ld >= R, tile
+  // stride RT), tile-major ones one panel per tile (ld = RT, tile stride at
+  // least rows x RT); a single tile is row-major
+  auto const layoutOk = [&](int64_t ld, int64_t ts) {
+    if (tiles == 1) return ld >= R;
+    return (ld >= R && ts == rt) || (ld == rt && ts >= rt);
+  };
+  if (!layoutOk(ldx, xTs) || !layoutOk(ldw, wTs)) return cudaErrorInvalidValue;
   dim3 grid((unsigned)(ctas * tiles));
   // one bulk copy per chunk: RT RHS with leading dimension RT, 16-byte aligned
-  int32_t const xBulk = ((R == rt && ldx == rt && (uintptr_t)X % 16 == 0) ? kTcBulkX : 0) |
-                        ((R == rt && (uintptr_t)W % 16 == 0) ? kTcBulkW : 0);
+  int32_t const xBulk =
+      ((ldx == rt && (uintptr_t)X % 16 == 0 && xTs % 2 == 0) ? kTcBulkX : 0) |
+      ((ldw == rt && (uintptr_t)W % 16 == 0 && wTs % 2 == 0) ? kTcBulkW : 0);
   auto const t32 = (int32_t)tiles;
   if (terms == 3 && rt == 16)
-    launchOne<3, 16>(grid, stream, chunks, ctaChunk0, tarena, X, ldx, W, R, t32, xBulk,
+    launchOne<3, 16>(grid, stream, chunks, ctaChunk0, tarena, X, ldx, xTs, W, ldw, wTs, R, t32, xBulk,
                      waitLimitNs, status);
   else if (terms == 3)
-    launchOne<3, 32>(grid, stream, chunks, ctaChunk0, tarena, X, ldx, W, R, t32, xBulk,
+    launchOne<3, 32>(grid, stream, chunks, ctaChunk0, tarena, X, ldx, xTs, W, ldw, wTs, R, t32, xBulk,
                      waitLimitNs, status);
   else if (rt == 16)
-    launchOne<2, 16>(grid, stream, chunks, ctaChunk0, tarena, X, ldx, W, R, t32, xBulk,
+    launchOne<2, 16>(grid, stream, chunks, ctaChunk0, tarena, X, ldx, xTs, W, ldw, wTs, R, t32, xBulk,
                      waitLimitNs, status);
   else
-    launchOne<2, 32>(grid, stream, chunks, ctaChunk0, tarena, X, ldx, W, R, t32, xBulk,
+    launchOne<2, 32>(grid, stream, chunks, ctaChunk0, tarena, X, ldx, xTs, W, ldw, wTs, R, t32, xBulk,
                      waitLimitNs, status);
   return cudaGetLastError();
 }

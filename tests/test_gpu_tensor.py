@@ -108,6 +108,33 @@ def test_tensor_apply_host_operands_and_original_order(ctx):
     assert rel_err(y_tree, g["y_bf"].reshape(y_tree.shape)) < TOL["bf16x3"]
 
 
+@pytest.mark.parametrize("R", [45, 64])
+def test_tensor_apply_host_operands_with_several_tiles(ctx, R):
+    """With more than one RHS tile the host-operand applies convert their
+    input straight into the tile-major layout (the device apply and the
+    original-order gather take it row-major): the same arithmetic, so the
+    same bits, for a partial last tile (45) and full tiles (64), through
+    the synchronous and the pipelined host calls."""
+    g, fac = golden_fac("star_n2048_k48", ctx)
+    sp, tp = fac.perms()
+    x = np.ascontiguousarray(O.RefRng(60 + R).complex_randn(2048 * R).reshape(2048, R))
+    y_dev = fac.apply(torch.from_numpy(x).cuda().to(torch.complex64),
+                      precision="bf16x3").cpu().numpy().astype(np.complex128)
+    y_host = fac.apply(x, precision="bf16x3")
+    assert np.array_equal(y_host, y_dev)
+    x_orig = np.empty_like(x)
+    x_orig[sp] = x
+    y_orig = fac.apply(x_orig, precision="bf16x3", original_order=True)
+    assert np.array_equal(y_orig[tp], y_host)
+    lib = B.lib()
+    xp = torch.from_numpy(x).pin_memory()
+    yp = torch.zeros((2048, R), dtype=torch.complex128).pin_memory()
+    ctx.check(lib.bfgFacApplyHostAsync(fac.handle, B.PRECISIONS["bf16x3"], B._VP(xp.data_ptr()),
+                                       R, R, B._VP(yp.data_ptr()), R, 0))
+    ctx.check(lib.bfgFacApplyHostWait(fac.handle))
+    assert np.array_equal(yp.numpy(), y_host)
+
+
 def test_tensor_apply_timed_launch_count(ctx):
     g, fac = golden_fac("star_n2048_k48", ctx)
     X = torch.zeros((2048, 16), dtype=torch.complex64, device="cuda")
