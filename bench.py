@@ -402,7 +402,7 @@ def batched_line(args, cfg, B, ctx, world, rank, local, dist):
     X, Y = precs[head]
     per = np.mean([fac.apply_timed(X.data_ptr(), R, R, Y.data_ptr(), R, head) for _ in range(3)],
                   axis=0)
-    info = fac.launch_info()
+    info = fac.launch_info(precision=head, rhs=R)
     dom = int(np.argmax(per))
     sA = {"fp64": 16, "df64": 16, "fp32": 8, "bf16x3": 12, "bf16x2": 8}[head]
     sv = 16 if head in ("fp64", "df64") else 8
@@ -836,17 +836,21 @@ def launch_roofline(fac, X, Y, R, prec):
     roof the dominant launch is closer to is the reported bound."""
     per = np.mean(np.array([fac.apply_timed(X.data_ptr(), R, R, Y.data_ptr(), R, prec)
                             for _ in range(3)], dtype=np.float64), axis=0)
-    info = fac.launch_info()
+    info = fac.launch_info(precision=prec, rhs=R)
     sA = ENTRY_BYTES[prec]
     sv = 16 if prec in ("fp64", "df64") else 8
     alg = [float(e * sA + R * sv * (ri + ro)) for e, ri, ro in info]
     dom = int(np.argmax(per))
+    # launches before the first stage (an input gather or tile-major copy:
+    # no stored entries)
+    lead = 1 if len(info) > 1 and info[0, 0] == 0 else 0
     hbm, bf16, src = measured_peaks()
     t = per[dom] / 1e3
     ach = float(alg[dom] / t / 1e9)
     alg_tf = float(8.0 * info[dom, 0] * R / t / 1e12)
     out = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
            "peak_source": src, "kernel": "apply launch %d of %d" % (dom, len(per)),
+           "stage": dom - lead if lead <= dom < len(per) - 1 else None,
            "launch_ms": float(per[dom]), "alg_bytes": alg[dom],
            "launch_share": [float(v) for v in per / per.sum()],
            "alg_bytes_per_launch": alg, "launch_ms_all": [float(v) for v in per],
@@ -1025,7 +1029,7 @@ def run_profile(args):
         fac.apply_device(X.data_ptr(), R, R, Y.data_ptr(), R, args.profile)
     torch.cuda.synchronize()
     per = fac.apply_timed(X.data_ptr(), R, R, Y.data_ptr(), R, args.profile)
-    info = fac.launch_info()
+    info = fac.launch_info(precision=args.profile, rhs=R)
     print(json.dumps({"workload": args.config, "rhs": R, "precision": args.profile,
                       "factorization_s": wall, "launches_per_apply": len(info),
                       "entries_per_launch": [int(v) for v in info[:, 0]],
@@ -1145,9 +1149,9 @@ def main():
     ratios = NCU_DRAM_PER_ALG.get((args.config, head, R))
     roof["traffic"] = None
     if ratios is not None:
-        dom = int(roof["kernel"].split()[2])
-        if dom < len(ratios):
-            roof["traffic"] = float(ratios[dom] * roof["alg_bytes"])
+        st = roof["stage"]
+        if st is not None and st < len(ratios):
+            roof["traffic"] = float(ratios[st] * roof["alg_bytes"])
             roof["traffic_source"] = NCU_TRAFFIC_SOURCE[(args.config, R)]
 
     # end to end through the C ABI with pinned host complex128 operands, two
@@ -1209,7 +1213,7 @@ def main():
                            (rows, yd), Xh, dist) if rank == 0 else None
     fac_info = fac_summary(fac, fac_wall_s)
     plan_text = fac.describe()
-    launches = len(fac.launch_info()) * steps_p[head]
+    launches = len(fac.launch_info(precision=head, rhs=R)) * steps_p[head]
     fac.close()
     del precs, X64, X32, Y64, Y32, Y16, Ydf, X, Y
     torch.cuda.empty_cache()

@@ -141,6 +141,8 @@ def lib() -> ctypes.CDLL:
         "bfgFacAutotune": [_VP, ctypes.c_int32, _I64, _VP, ctypes.c_int32,
                            ctypes.POINTER(ctypes.c_int32)],
         "bfgFacGetRhsTile": [_VP, ctypes.c_int32, _I64, ctypes.POINTER(ctypes.c_int32)],
+        "bfgFacGetApplyLaunches": [_VP, ctypes.c_int32, _I64, ctypes.c_uint32, _VP,
+                                   ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)],
         "bfgQuadtreeBuild": [_VP, _VP, _VP, _I64, _I64, ctypes.c_int32, _VP, _VP, _I64, _VP],
         "bfgRngSeed": [ctypes.POINTER(_RngC), ctypes.c_uint64],
         "bfgRngUniform1": [ctypes.POINTER(_RngC)],
@@ -518,13 +520,16 @@ class Fac:
         bounded wait (bfgFacSynchronize)."""
         self.ctx.check(lib().bfgFacSynchronize(self.handle), "synchronize")
 
-    def launch_info(self, original_order: bool = False) -> np.ndarray:
-        """(entries, rows_in, rows_out) per launch of one apply."""
+    def launch_info(self, original_order: bool = False, precision: str = "fp64",
+                    rhs: int = 1) -> np.ndarray:
+        """(entries, rows_in, rows_out) per launch of one apply in this
+        precision with `rhs` right-hand sides (bfgFacGetApplyLaunches)."""
         cap = 256
         info = np.zeros((cap, 3), dtype=np.int64)
         n = ctypes.c_int32()
-        self.ctx.check(lib().bfgFacGetLaunchInfo(
-            self.handle, APPLY_ORIGINAL_ORDER if original_order else 0, _ptr(info), cap,
+        self.ctx.check(lib().bfgFacGetApplyLaunches(
+            self.handle, PRECISIONS[precision], int(rhs),
+            APPLY_ORIGINAL_ORDER if original_order else 0, _ptr(info), cap,
             ctypes.byref(n)), "launch_info")
         return info[:n.value].copy()
 

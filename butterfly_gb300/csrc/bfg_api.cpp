@@ -651,8 +651,21 @@ void runApply(bfgFac f, T2 const *arena, T2 const *X, int64_t ldx, int64_t R, T2
   mark();
 }
 
-size_t numApplyLaunches(bfgFac f, uint32_t flags) {
-  return (f->stageItem0.size() - 1) + 1 + ((flags & BFG_APPLY_ORIGINAL_ORDER) ? 1 : 0);
+int32_t tcTile(bfgFac_s::Tc const &tc, int64_t R);
+bool isTcPrecision(bfgPrecision p);
+
+// a tensor-core apply of more than one RHS tile copies its input tile-major
+// first (the original-order gather does that on its way)
+bool tcTiledCopy(bfgFac f, bfgPrecision prec, int64_t R, uint32_t flags) {
+  return isTcPrecision(prec) && !(flags & BFG_APPLY_ORIGINAL_ORDER) &&
+         R > tcTile(f->tc[prec == BFG_PRECISION_BF16X3 ? 1 : 0], R);
+}
+
+// launches of one device-operand apply: an input gather or copy, the
+// stages, the final sum
+size_t numApplyLaunches(bfgFac f, uint32_t flags, bfgPrecision prec, int64_t R) {
+  bool const copy = (flags & BFG_APPLY_ORIGINAL_ORDER) || tcTiledCopy(f, prec, R, flags);
+  return (f->stageItem0.size() - 1) + 1 + (copy ? 1 : 0);
 }
 
 void ensureArena32(bfgFac f) {
@@ -843,6 +856,19 @@ void runApplyTc(bfgFac f, int terms, float2 const *X, int64_t ldx, int64_t R, fl
     if (events) ck(cudaEventRecord((*events)[ev++], s), "event");
   };
   mark();
+  if (tiled && !xTiled && !(flags & BFG_APPLY_ORIGINAL_ORDER)) {
+    // the caller's row-major input copied tile-major, so that the first
+    // stage too bulk-copies its input rows (one launch; the stage's
+    // cp.async copies took 14 % more time than bulk copies)
+    ck(f->xbuf.ensure((size_t)p.numCols * tiles * rt * sizeof(float2)), "input buffer");
+    ck(bfg::launchGatherRows<float2>(X, ldx, nullptr, p.numCols, R, f->xbuf.as<float2>(), s, rt,
+                                     p.numCols * rt),
+       "tile-major input");
+    Xt = f->xbuf.as<float2>();
+    ldxt = rt;
+    xTs = p.numCols * rt;
+    mark();
+  }
   if (flags & BFG_APPLY_ORIGINAL_ORDER) {
     ck(f->xbuf.ensure((size_t)p.numCols * (tiled ? tiles * rt : R) * sizeof(float2)),
        "gather buffer");
@@ -1483,7 +1509,7 @@ bfgStatus bfgFacApplyTimed(bfgFac f, bfgPrecision prec, void const *X, int64_t l
                            int32_t *numLaunches) {
   if (!f || !numLaunches) return BFG_ERROR_INVALID_ARGUMENTS;
   return guarded(f->ctx, [&]() -> bfgStatus {
-    size_t const n = numApplyLaunches(f, flags);
+    size_t const n = numApplyLaunches(f, flags, prec, R);
     *numLaunches = (int32_t)n;
     if (!ms || cap < (int32_t)n) return fail(f->ctx, BFG_ERROR_OUT_OF_RANGE, "timed apply: buffer too small");
     preparePrecision(f, prec);
@@ -1498,15 +1524,17 @@ bfgStatus bfgFacApplyTimed(bfgFac f, bfgPrecision prec, void const *X, int64_t l
   });
 }
 
-bfgStatus bfgFacGetLaunchInfo(bfgFac f, uint32_t flags, int64_t *info, int32_t cap,
-                              int32_t *numLaunches) {
-  if (!f || !numLaunches) return BFG_ERROR_INVALID_ARGUMENTS;
-  size_t const n = numApplyLaunches(f, flags);
+bfgStatus bfgFacGetApplyLaunches(bfgFac f, bfgPrecision prec, int64_t R, uint32_t flags,
+                                 int64_t *info, int32_t cap, int32_t *numLaunches) {
+  if (!f || !numLaunches || R < 1) return BFG_ERROR_INVALID_ARGUMENTS;
+  if (prec < BFG_PRECISION_FP64 || prec > BFG_PRECISION_DF64)
+    return fail(f->ctx, BFG_ERROR_INVALID_ARGUMENTS, "launch info: unknown precision");
+  size_t const n = numApplyLaunches(f, flags, prec, R);
   *numLaunches = (int32_t)n;
   if (!info || cap < (int32_t)n) return fail(f->ctx, BFG_ERROR_OUT_OF_RANGE, "launch info: buffer too small");
   bfg::ApplyProgram const &p = f->prog;
   size_t k = 0;
-  if (flags & BFG_APPLY_ORIGINAL_ORDER) {
+  if ((flags & BFG_APPLY_ORIGINAL_ORDER) || tcTiledCopy(f, prec, R, flags)) {
     info[3 * k] = 0;
     info[3 * k + 1] = p.numCols;
     info[3 * k + 2] = p.numCols;
@@ -1521,6 +1549,11 @@ bfgStatus bfgFacGetLaunchInfo(bfgFac f, uint32_t flags, int64_t *info, int32_t c
   info[3 * k + 1] = p.sumRows;
   info[3 * k + 2] = p.numRows;
   return BFG_OK;
+}
+
+bfgStatus bfgFacGetLaunchInfo(bfgFac f, uint32_t flags, int64_t *info, int32_t cap,
+                              int32_t *numLaunches) {
+  return bfgFacGetApplyLaunches(f, BFG_PRECISION_FP64, 1, flags, info, cap, numLaunches);
 }
 
 bfgStatus bfgFacApplyHost(bfgFac f, bfgPrecision prec, double const *X, int64_t ldx, int64_t R,
@@ -1615,15 +1648,16 @@ bfgStatus bfgFacAutotune(bfgFac f, bfgPrecision prec, int64_t R, double *stageMs
       }
       wd[w].best.assign(K, std::vector<float>(nStages, 1e30f));
     }
-    // scratch operands: the times do not depend on the values; the input
-    // row-major, the workspace laid out as the apply lays it out (tile-major
-    // with more than one tile)
+    // scratch operands: the times do not depend on the values; input and
+    // workspace laid out as the apply lays them out (tile-major with more
+    // than one tile)
     bfg::ApplyProgram const &p = f->prog;
     int64_t const wsRows = std::max<int64_t>(1, p.wsRows);
+    int64_t const cols32 = (R + 31) / 32 * 32;   // room for either tiling
     DevBuf xs;
-    ck(xs.ensure((size_t)std::max<int64_t>(1, p.numCols) * R * sizeof(float2)), "autotune");
-    ck(cudaMemsetAsync(xs.p, 0, (size_t)p.numCols * R * sizeof(float2), s), "autotune");
-    ck(f->ws.ensure((size_t)wsRows * ((R + 31) / 32) * 32 * sizeof(float2)), "workspace");
+    ck(xs.ensure((size_t)std::max<int64_t>(1, p.numCols) * cols32 * sizeof(float2)), "autotune");
+    ck(cudaMemsetAsync(xs.p, 0, (size_t)p.numCols * cols32 * sizeof(float2), s), "autotune");
+    ck(f->ws.ensure((size_t)wsRows * cols32 * sizeof(float2)), "workspace");
     Events const ev(nStages + 1, "autotune");
     int const reps = 5;
     DevBuf dch, dc0;
@@ -1637,9 +1671,10 @@ bfgStatus bfgFacAutotune(bfgFac f, bfgPrecision prec, int64_t R, double *stageMs
             bool const tiled = R > w.rt;
             ck(bfg::launchApplyTc(terms, w.rt, dch.as<bfg::TcChunk>(),
                                   dc0.as<int64_t>() + st * (size_t)(w.ctas + 1), w.ctas,
-                                  tc.arena.as<uint8_t>(), xs.as<float2>(), R, w.rt,
-                                  f->ws.as<float2>(), tiled ? w.rt : R,
-                                  tiled ? wsRows * w.rt : w.rt, R, f->tcStatus.as<int32_t>(), s),
+                                  tc.arena.as<uint8_t>(), xs.as<float2>(), tiled ? w.rt : R,
+                                  tiled ? p.numCols * w.rt : w.rt, f->ws.as<float2>(),
+                                  tiled ? w.rt : R, tiled ? wsRows * w.rt : w.rt, R,
+                                  f->tcStatus.as<int32_t>(), s),
                "autotune");
             ck(cudaEventRecord(ev[st + 1], s), "autotune");
           }

@@ -1033,7 +1033,7 @@ __global__ void gatherRowsKernel(T2 const *X, int64_t ldx, int64_t const *perm,
        e += (int64_t)gridDim.x * blockDim.x) {
     int64_t const i = e / R, r = e % R;
     int64_t const o = outTile ? (r / outTile) * outTileStride + i * outTile + r % outTile : e;
-    out[o] = X[perm[i] * ldx + r];
+    out[o] = X[(perm ? perm[i] : i) * ldx + r];
   }
 }
 

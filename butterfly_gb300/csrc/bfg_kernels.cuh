@@ -180,7 +180,7 @@ cudaError_t launchApplyTc(int32_t terms, int32_t rt, TcChunk const *chunks,
                           uint64_t waitLimitNs = kTcWaitLimitNs);
 enum : int32_t { kStatusTcTimeout = 4 };
 
-// X_tree[i] = X[perm[i]] (row gather, R columns) into out row-major
+// X_tree[i] = X[perm[i]] (row gather, R columns; no perm: X[i]) into out row-major
 // (leading dimension R) or (outTile > 0) tile-major: panel t of outTile
 // columns at out + t outTileStride, leading dimension outTile
 template <typename T2>

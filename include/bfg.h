@@ -311,9 +311,20 @@ bfgStatus bfgFacApplyTimed(bfgFac fac, bfgPrecision precision, void const *X,
                            uint32_t flags, float *launchMs, int32_t capacity,
                            int32_t *numLaunches);
 
-/* Algorithmic work of each launch of an apply with these flags, in the
+/* Algorithmic work of each launch of a device-operand apply (bfgFacApply)
+ * in this precision with numRhs right-hand sides and these flags, in the
  * order of bfgFacApplyTimed: info[3i..3i+2] = stored complex entries read,
- * vector rows read, vector rows written (per right-hand side). */
+ * vector rows read, vector rows written (per right-hand side).  The
+ * launches: the input's gather (original order) or, for a tensor-core
+ * apply of more than one RHS tile, its tile-major copy; the stages; the
+ * final sum. */
+bfgStatus bfgFacGetApplyLaunches(bfgFac fac, bfgPrecision precision, int64_t numRhs,
+                                 uint32_t flags, int64_t *info, int32_t capacity,
+                                 int32_t *numLaunches);
+
+/* bfgFacGetApplyLaunches for the applies whose launches do not depend on
+ * the precision or the right-hand-side count: FP64, FP32, DF64, and the
+ * tensor-core applies of one RHS tile. */
 bfgStatus bfgFacGetLaunchInfo(bfgFac fac, uint32_t flags, int64_t *info,
                               int32_t capacity, int32_t *numLaunches);
 

@@ -135,13 +135,25 @@ def test_tensor_apply_host_operands_with_several_tiles(ctx, R):
     assert np.array_equal(yp.numpy(), y_host)
 
 
-def test_tensor_apply_timed_launch_count(ctx):
+@pytest.mark.parametrize("R", [16, 64])
+def test_tensor_apply_timed_launch_count(ctx, R):
+    """One tile: the stages and the final sum; more tiles: the input's
+    tile-major copy first (no stored entries, every input row)."""
     g, fac = golden_fac("star_n2048_k48", ctx)
-    X = torch.zeros((2048, 16), dtype=torch.complex64, device="cuda")
+    X = torch.zeros((2048, R), dtype=torch.complex64, device="cuda")
     Y = torch.empty_like(X)
     torch.cuda.synchronize()
-    ms = fac.apply_timed(X.data_ptr(), 16, 16, Y.data_ptr(), 16, "bf16x3")
-    assert len(ms) == len(fac.launch_info())
+    ms = fac.apply_timed(X.data_ptr(), R, R, Y.data_ptr(), R, "bf16x3")
+    info = fac.launch_info(precision="bf16x3", rhs=R)
+    assert len(ms) == len(info)
+    stages = len(fac.launch_info()) - 1
+    if R <= 32:
+        assert len(info) == stages + 1
+        assert np.array_equal(info, fac.launch_info())
+    else:
+        assert len(info) == stages + 2
+        assert info[0, 0] == 0 and info[0, 1] == info[0, 2] == 2048
+        assert np.array_equal(info[1:], fac.launch_info())
     assert torch.count_nonzero(Y).item() == 0
 
 
