@@ -61,8 +61,8 @@ NCU_DRAM_PER_ALG = {("c2", "fp32", 16): [0.7973, 1.0266, 0.9855, 0.7925],
                     ("c2", "bf16x3", 16): [0.8888, 1.0627, 1.0246, 1.0386],
                     ("c2s", "fp32", 16): [0.7973, 1.0266, 0.9855, 0.7925],
                     ("c2s", "bf16x3", 16): [0.8888, 1.0627, 1.0246, 1.0386],
-                    ("c2", "bf16x3", 256): [0.538, 1.057],
-                    ("c4", "bf16x3", 256): [0.538, 1.057]}
+                    ("c2", "bf16x3", 256): [0.537, 1.057],
+                    ("c4", "bf16x3", 256): [0.537, 1.057]}
 NCU_TRAFFIC_SOURCE = {
     ("c2", 16): "ncu DRAM bytes of the same stage in a capture of the 32,768-point workload, "
                 "scaled by algorithmic bytes",
