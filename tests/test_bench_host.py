@@ -103,3 +103,45 @@ def test_standin_port_over_a_plan_with_wrapped_values():
     full = O.ApplyPort.from_plan(text, np.full(entries, 1e-3 + 0j), True)
     X = O.RefRng(2).complex_randn(2048 * 2).reshape(2048, 2)
     assert np.allclose(port(X, 2), full(X, 2), rtol=1e-13, atol=0)
+
+
+class _FakeFac:
+    """Per-launch times and launch info of a tensor-core apply of several
+    RHS tiles: the input's tile-major copy, three stages, the final sum."""
+    def __init__(self, ms, info):
+        self.ms, self.info = np.asarray(ms, dtype=np.float32), np.asarray(info, dtype=np.int64)
+
+    def apply_timed(self, *args):
+        return self.ms
+
+    def launch_info(self, **kw):
+        return self.info
+
+
+class _Ptr:
+    def data_ptr(self):
+        return 0
+
+
+def test_launch_roofline_maps_the_dominant_launch_to_its_stage():
+    """The roofline's dominant launch is reported with its stage index (the
+    input copy before the first stage has no stored entries), which selects
+    the ncu DRAM ratio; the algorithmic bytes and rates follow the launch
+    info."""
+    R = 256
+    info = [[0, 1000, 1000], [5000, 1000, 300], [4000, 300, 200], [0, 500, 1000]]
+    fac = _FakeFac([0.1, 2.0, 1.5, 0.05], info)
+    roof = bench.launch_roofline(fac, _Ptr(), _Ptr(), R, "bf16x3")
+    assert roof["kernel"] == "apply launch 1 of 4" and roof["stage"] == 0
+    alg = 5000 * 12 + R * 8 * (1000 + 300)
+    assert roof["alg_bytes"] == alg
+    assert np.isclose(roof["launch_ms"], 2.0)
+    assert np.isclose(roof["hbm"]["achieved_gbs"], alg / 2e-3 / 1e9)
+    assert np.isclose(roof["tensor"]["achieved_alg_tflops"], 8 * 5000 * R / 2e-3 / 1e12)
+    assert np.isclose(sum(roof["launch_share"]), 1.0)
+    # no copy launch: the stage index is the launch index; the final sum
+    # has no stage
+    fac = _FakeFac([2.0, 1.5, 0.05], info[1:])
+    assert bench.launch_roofline(fac, _Ptr(), _Ptr(), R, "bf16x3")["stage"] == 0
+    fac = _FakeFac([0.1, 0.2, 3.0], info[1:])
+    assert bench.launch_roofline(fac, _Ptr(), _Ptr(), R, "fp32")["stage"] is None
