@@ -102,6 +102,14 @@ def test_host_entry_points_reject_bad_input():
         B.plan_helm2(-1.0, np.zeros((4, 2)), np.ones((4, 2)))
     with pytest.raises(ValueError):
         B.plan_helm2(1.0, np.zeros((4, 3)), np.ones((4, 2)))
+    # empty point sets are refused, not planned (the reference's tree build
+    # has no empty case)
+    pts = B.uniform_square_points(10, 3)
+    for src, tgt in ((pts[:0], pts), (pts, pts[:0]), (pts[:0], pts[:0])):
+        with pytest.raises(B.BfgError):
+            B.plan_helm2(10.0, src, tgt)
+        with pytest.raises(B.BfgError):
+            B.check_apply_schedule([(10.0, src, tgt)])
 
 
 # every struct the Python mirror passes across the C ABI, by its C name
